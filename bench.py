@@ -1,0 +1,334 @@
+"""Benchmark: the plain large workload, one frame per step.
+
+Workload (the large plain configuration): a 1,003,520-face geodesic
+icosphere (nu=224) with seeded radial displacement, FP32; LBVH build from
+the resident vertices, then a 1920x1080 render at 16 samples per pixel with
+a thin lens (aperture radius 0.05, focus 3.0) on the reference's mrand
+stream, Lambert shading and one shadow ray per hit.  A step = crt_bvh_build
++ crt_render (device buffers).  `value` = primary rays per second of the
+whole step (1920*1080*16 / step time), in Mrays/s.
+
+`e2e` runs the same step through the C ABI with host buffers: the vertex
+upload from pinned memory (crt_scene_set_vertices, rebuild) and the image
+download into pinned memory (crt_render with a host rgb8 pointer).
+
+L2 (129 MB) is flushed between timed steps by writing a 512 MB buffer
+outside the timed region; each step is timed alone with CUDA events on the
+stream the library launches on, and the step times are summed.
+
+`--impl reference` times the reference's algorithm on the host cores: the
+reference's own device code compiled for the host (oracle/_ref) where it
+was built for this machine, else the oracle port (oracle/crt_oracle.cpp),
+with all host threads, on a bounded sample of the same workload (a band of
+image rows per step, the BVH built once outside the timed region).
+
+Multi-GPU (torchrun): independent replicas, one frame per rank per step; the
+barrier + max-over-ranks timing gives the whole-job rate.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "cuda-rt_gb300"))
+sys.path.insert(0, ROOT)
+
+METRIC = "LBVH build Mtris/s; closest-hit Mrays/s; batched+adjoint vs plain, 1 GB300"
+W, H, SPP = 1920, 1080, 16
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples nvidia-smi during the timed region."""
+
+    def __init__(self, index=0):
+        self.samples, self.proc, self.index = [], None, index
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if "Active" in s[3 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl" if os.environ.get("CRT_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+        dist.init_process_group(backend)
+        return dist, rank, ws
+    return None, 0, 1
+
+
+def max_over_ranks(dist, x, device="cpu"):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def run_crt(args, dist, rank, ws):
+    import torch
+
+    import crt
+    from crt import data
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    sc = data.config1()
+    mesh = sc.mesh
+    n = mesh.ntri
+    scene = crt.Scene(mesh)
+    stream = torch.cuda.current_stream()
+    rgb = torch.empty((W * H, 3), dtype=torch.uint8, device="cuda")
+    out = {"rgb8": rgb}
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    def step():
+        scene.build(stream=stream)
+        scene.render(sc.camera, sc.light, W, H, SPP, out=out, stream=stream)
+
+    # warm-up
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    scene.check()
+    # instrumented pass (outside timing): traversal traffic for the roofline
+    stats = torch.zeros(2, dtype=torch.int64, device="cuda")
+    scene.render(sc.camera, sc.light, W, H, SPP, out={"rgb8": rgb, "traversal_stats": stats}, stream=stream)
+    torch.cuda.synchronize()
+    nodes_visited, tris_tested = [int(x) for x in stats.cpu()]
+    # timed steps: build and render timed separately, L2 flushed before each step
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    barrier(dist)
+    torch.cuda.synchronize()
+    with Clocks(dev) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            scene.build(stream=stream)
+            ev[k][1].record(stream)
+            scene.render(sc.camera, sc.light, W, H, SPP, out=out, stream=stream)
+            ev[k][2].record(stream)
+        torch.cuda.synchronize()
+    barrier(dist)
+    t_build = sum(e[0].elapsed_time(e[1]) for e in ev) / 1e3
+    t_render = sum(e[1].elapsed_time(e[2]) for e in ev) / 1e3
+    t_total = max_over_ranks(dist, t_build + t_render, "cuda")
+    rays = W * H * SPP
+    value = rays * args.steps * ws / t_total / 1e6
+    ms_step = t_total / args.steps * 1e3
+    hbm, peak_kind = peaks()
+    # render roofline (the dominant kernel): 64 B per visited internal node +
+    # 36 B per tested triangle (the fixed traffic model), per launch
+    alg_bytes = nodes_visited * 64 + tris_tested * 36
+    render_s = t_render / args.steps
+    achieved = alg_bytes / render_s / 1e9
+    build_s = t_build / args.steps
+    s_in = 12 + 12 * mesh.verts.shape[0] / n
+    build_bytes = n * (s_in + 220)
+    scene.check()
+
+    # e2e through the C ABI with host (pinned) buffers
+    verts_h = torch.from_numpy(mesh.verts).pin_memory()
+    rgb_h = torch.empty((W * H, 3), dtype=torch.uint8).pin_memory()
+    out_h = {"rgb8": rgb_h}
+
+    def e2e_step():
+        scene.set_vertices(verts_h, rebuild=True, stream=stream)
+        scene.render(sc.camera, sc.light, W, H, SPP, out=out_h, stream=stream)
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_steps = max(3, args.steps // 2)
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    t_e2e = max_over_ranks(dist, time.perf_counter() - t0, "cuda")
+    e2e_value = rays * e2e_steps * ws / t_e2e / 1e6
+    ok_img = bool(np.array_equal(rgb_h.numpy(), rgb.cpu().numpy()))
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(sc, args.cpu_seconds)
+    if rank != 0:
+        return None
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded icosphere, PCG64)",
+        "config": {"workload": "large plain: nu=224 icosphere 1,003,520 tris FP32, LBVH build + 1920x1080 "
+                               "16 spp thin-lens render (aperture 0.05, focus 3.0), Lambert + 1 shadow ray/hit",
+                   "triangles": n, "width": W, "height": H, "spp": SPP,
+                   "l2": "flushed between steps (512 MB write, untimed)", "parallelism": f"replicas x{ws}"},
+        "build_mtris_s": round(n / build_s / 1e6, 2), "build_ms": round(build_s * 1e3, 4),
+        "render_ms": round(render_s * 1e3, 3), "render_mrays_s": round(rays / render_s / 1e6, 2),
+        "build_roofline": {"bound": "hbm", "achieved": round(build_bytes / build_s / 1e9, 1), "peak": hbm,
+                           "unit": "GB/s", "frac": round(build_bytes / build_s / 1e9 / hbm, 4),
+                           "bytes_per_tri": round(s_in + 220, 1), "peak_kind": peak_kind},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 4), "traffic": None, "kernel": "k_render",
+                     "alg_bytes_per_launch": alg_bytes, "nodes_visited": nodes_visited,
+                     "tris_tested": tris_tested, "peak_kind": peak_kind},
+        "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(mesh.verts.nbytes),
+                "d2h_bytes_per_step": W * H * 3, "image_matches_device_run": ok_img},
+        "gpu_launches": 9 * args.steps,
+        "clocks": clk.summary(),
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    return line
+
+
+def _cpu_impl():
+    from oracle import oracle as orc
+    kind = "port"
+    try:
+        if orc.ref_available():
+            import ctypes
+            ctypes.CDLL(orc.REF_LIB)
+            kind = "reference"
+    except OSError:
+        kind = "port"
+    return kind
+
+
+def cpu_baseline(sc, seconds):
+    """The reference algorithm on the host cores for a band of rows of the
+    same frame; Mrays/s of primary rays (each with its shadow ray)."""
+    from oracle.oracle import OracleScene
+    kind = _cpu_impl()
+    cores = os.cpu_count() or 1
+    o = OracleScene(sc.mesh, "ref" if kind == "reference" else "oracle")
+    spp = 20 if kind == "reference" else SPP  # the reference's kernel always takes 20
+    rows, done, t_used = 16, 0, 0.0
+    r0 = H // 2 - 8
+    while t_used < seconds and done < H:
+        a = max(0, min(r0, H - rows))
+        t0 = time.perf_counter()
+        o.render(sc.camera, sc.light, W, H, spp=None if kind == "reference" else spp, rows=(a, a + rows))
+        t_used += time.perf_counter() - t0
+        done += rows
+        r0 = (r0 + 97) % (H - rows)
+    value = done * W * spp / t_used / 1e6
+    return {"value": round(value, 4), "unit": "Mrays/s", "cores": cores, "kind": kind,
+            "sample": f"{done} rows of {W} px x {spp} spp (bands of 16 rows) of the {W}x{H} frame, "
+                      f"BVH built once untimed, {t_used:.1f} s"}
+
+
+def run_reference(args, dist, rank, ws):
+    from crt import data
+    from oracle.oracle import OracleScene
+    if rank != 0:
+        return None
+    kind = _cpu_impl()
+    sc = data.config1()
+    o = OracleScene(sc.mesh, "ref" if kind == "reference" else "oracle")
+    spp = 20 if kind == "reference" else SPP
+    rows = 4
+    times = []
+    for k in range(args.warmup + args.steps):
+        a = (H // 2 - 2 + 37 * k) % (H - rows)
+        t0 = time.perf_counter()
+        o.render(sc.camera, sc.light, W, H, spp=None if kind == "reference" else spp, rows=(a, a + rows))
+        if k >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    t = sum(times)
+    value = rows * W * spp * len(times) / t / 1e6
+    cores = os.cpu_count() or 1
+    sample = f"{rows} rows x {W} px x {spp} spp per step of the {W}x{H} frame, BVH built once untimed"
+    return {"metric": METRIC, "value": round(value, 4), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(t / len(times) * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded icosphere, PCG64)",
+            "config": {"workload": "large plain: nu=224 icosphere 1,003,520 tris FP32, 1920x1080 thin-lens render, "
+                                   "Lambert + 1 shadow ray/hit (row-band sample)", "triangles": sc.mesh.ntri},
+            "impl": "reference",
+            "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": cores, "kind": kind,
+                             "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="crt", choices=["crt", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "crt" else args.warmup
+    dist, rank, ws = dist_setup()
+    if args.impl == "reference":
+        line = run_reference(args, dist, rank, ws)
+    else:
+        import __graft_entry__
+        if rank == 0:
+            __graft_entry__.build()
+        barrier(dist)
+        line = run_crt(args, dist, rank, ws)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,247 @@
+"""Python front end of libcrt.so (the C ABI in include/crt.h), via ctypes.
+
+The names mirror the reference's host API (inc/raytracer.h, inc/scene.h,
+inc/camera.h, inc/Light.h): a ``Scene`` is Scene_d with its BVH_d, built on
+construction like ``Scene_d::operator=(const Scene_h&)``; ``render`` is
+RayTracer::run + pullRaytracedImage.  Buffers may be NumPy arrays (host) or
+torch CUDA tensors (device); the library copies as needed.
+
+The CUDA library is required: importing ``crt`` raises if libcrt.so is
+missing, and nothing here falls back to a CPU implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+from . import data  # noqa: F401
+from .build import LIB as LIB_PATH
+
+__all__ = ["CrtError", "Scene", "lib", "sort_pairs", "morton", "STATUS", "render_args"]
+
+STATUS = {0: "CRT_OK", 1: "CRT_INVALID_ARG", 2: "CRT_OOM", 3: "CRT_CUDA_ERROR", 4: "CRT_STACK_OVERFLOW",
+          5: "CRT_TIMEOUT", 6: "CRT_NOT_BUILT"}
+
+
+class CrtError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class _Material(C.Structure):
+    _fields_ = [("ka", C.c_double * 3), ("kd", C.c_double * 3), ("ks", C.c_double * 3), ("kt", C.c_double * 3),
+                ("ke", C.c_double * 3), ("shininess", C.c_double)]
+
+
+class _MeshDesc(C.Structure):
+    _fields_ = [("vertices", C.c_void_p), ("num_vertices", C.c_int32), ("normals", C.c_void_p),
+                ("num_normals", C.c_int32), ("vertex_indices", C.c_void_p), ("normal_indices", C.c_void_p),
+                ("num_triangles", C.c_int32), ("materials", C.c_void_p), ("num_materials", C.c_int32),
+                ("material_ids", C.c_void_p)]
+
+
+class _Camera(C.Structure):
+    _fields_ = [("fov", C.c_double), ("focal_point", C.c_double), ("fstop", C.c_double), ("eye", C.c_double * 3)]
+
+
+class _Light(C.Structure):
+    _fields_ = [("color", C.c_double * 3), ("position", C.c_double * 3), ("radius", C.c_double),
+                ("constant_term", C.c_double), ("linear_term", C.c_double), ("quadratic_term", C.c_double)]
+
+
+class _RenderParams(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("row_begin", C.c_int32),
+                ("row_end", C.c_int32)]
+
+
+class _RenderOut(C.Structure):
+    _fields_ = [("rgb8", C.c_void_p), ("rgb_f32", C.c_void_p), ("hit_id", C.c_void_p), ("hit_t", C.c_void_p),
+                ("shadow", C.c_void_p), ("rays", C.c_void_p), ("traversal_stats", C.c_void_p)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libcrt.so (build it first with ``__graft_entry__.build()``)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libcrt.so not built ({LIB_PATH}); run __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        vp, i32, i64 = C.c_void_p, C.c_int32, C.c_int64
+        sig = {
+            "crt_scene_create": [vp, vp, vp],
+            "crt_scene_destroy": [vp],
+            "crt_scene_set_vertices": [vp, vp, C.c_int, vp],
+            "crt_bvh_build": [vp, vp],
+            "crt_bvh_refit": [vp, vp],
+            "crt_bvh_export": [vp, vp, vp, vp, vp, vp, vp],
+            "crt_trace_closest": [vp, vp, i64, vp, vp, vp, vp],
+            "crt_trace_shadow": [vp, vp, i64, vp, vp, vp],
+            "crt_render": [vp, vp, vp, vp, vp, vp],
+            "crt_morton": [vp, vp, i32, vp, vp, vp],
+            "crt_sort_pairs": [vp, vp, vp, vp, i32, i32, vp],
+            "crt_scene_check": [vp, vp],
+        }
+        for name, args in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = C.c_int
+        L.crt_last_error_string.restype = C.c_char_p
+        L.crt_version.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+def _check(status):
+    if status != 0:
+        raise CrtError(status, lib().crt_last_error_string().decode())
+
+
+def _addr(a):
+    """Address of a NumPy array or torch tensor (None -> NULL)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        assert a.flags["C_CONTIGUOUS"]
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        assert a.is_contiguous()
+        return a.data_ptr()
+    raise TypeError(type(a))
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    if hasattr(stream, "cuda_stream"):
+        return stream.cuda_stream
+    return int(stream)
+
+
+class Scene:
+    """Scene_d + BVH_d: a mesh on the GPU with its LBVH (built on construction)."""
+
+    def __init__(self, mesh, stream=None):
+        self._keep = []
+
+        def hold(a, dt):
+            if a is None:
+                return None
+            if isinstance(a, np.ndarray):
+                a = np.ascontiguousarray(a, dt)
+            self._keep.append(a)
+            return _addr(a)
+
+        mats = np.ascontiguousarray(np.asarray(mesh.materials, np.float64).reshape(-1, 16))
+        self.ntri = int(mesh.vidx.shape[0])
+        self.nv = int(mesh.verts.shape[0])
+        d = _MeshDesc(hold(mesh.verts, np.float32), self.nv, hold(mesh.normals, np.float32),
+                      int(mesh.normals.shape[0]), hold(mesh.vidx, np.int32), hold(mesh.nidx, np.int32), self.ntri,
+                      hold(mats, np.float64), int(mats.shape[0]), hold(mesh.matid, np.int32))
+        h = C.c_void_p()
+        _check(lib().crt_scene_create(C.byref(d), _stream(stream), C.byref(h)))
+        self.h = h
+        self._keep = []
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().crt_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_vertices(self, verts, rebuild: bool, stream=None):
+        if isinstance(verts, np.ndarray):
+            verts = np.ascontiguousarray(verts, np.float32)
+        _check(lib().crt_scene_set_vertices(self.h, _addr(verts), int(bool(rebuild)), _stream(stream)))
+
+    def build(self, stream=None):
+        _check(lib().crt_bvh_build(self.h, _stream(stream)))
+
+    def refit(self, stream=None):
+        _check(lib().crt_bvh_refit(self.h, _stream(stream)))
+
+    def check(self, stream=None):
+        _check(lib().crt_scene_check(self.h, _stream(stream)))
+
+    def export(self) -> dict:
+        n = self.ntri
+        nn = max(2 * n - 1, 0)
+        out = dict(scene_box=np.zeros(6, np.float32), codes=np.zeros(n, np.int32), ids=np.zeros(n, np.uint32),
+                   nodes=np.zeros((nn, 3), np.int32), node_boxes=np.zeros((nn, 6), np.float32))
+        _check(lib().crt_bvh_export(self.h, *[_addr(out[k]) for k in ("scene_box", "codes", "ids", "nodes",
+                                                                        "node_boxes")], None))
+        return out
+
+    def trace(self, rays, any_hit=False, normals=False, stream=None):
+        """rays: (n, 6) float64 (NumPy or CUDA tensor).  Returns ids, t[, normals]."""
+        n = int(rays.shape[0])
+        if isinstance(rays, np.ndarray):
+            rays = np.ascontiguousarray(rays, np.float64)
+            ids, t = np.zeros(n, np.int32), np.zeros(n, np.float64)
+            nrm = np.zeros((n, 3), np.float64) if normals and not any_hit else None
+        else:
+            import torch
+            ids = torch.empty(n, dtype=torch.int32, device=rays.device)
+            t = torch.empty(n, dtype=torch.float64, device=rays.device)
+            nrm = torch.empty((n, 3), dtype=torch.float64, device=rays.device) if normals and not any_hit else None
+        if any_hit:
+            _check(lib().crt_trace_shadow(self.h, _addr(rays), n, _addr(ids), _addr(t), _stream(stream)))
+        else:
+            _check(lib().crt_trace_closest(self.h, _addr(rays), n, _addr(ids), _addr(t), _addr(nrm),
+                                           _stream(stream)))
+        return (ids, t, nrm) if normals and not any_hit else (ids, t)
+
+    def render(self, camera, light, width, height, spp, rows=None, out=None, aux=False, rays=False, rgbf=False,
+               stream=None):
+        """RayTracer::run + pullRaytracedImage.  Returns a dict of NumPy
+        arrays unless `out` (a dict of preallocated buffers) is given."""
+        cam, lt, p = render_args(camera, light, width, height, spp, rows)
+        if out is None:
+            npx, ns = width * height, width * height * spp
+            out = dict(rgb8=np.zeros((npx, 3), np.uint8))
+            if rgbf:
+                out["rgb_f32"] = np.zeros((npx, 3), np.float32)
+            if aux:
+                out.update(hit_id=np.zeros(ns, np.int32), hit_t=np.zeros(ns, np.float64),
+                           shadow=np.zeros(ns, np.int32))
+            if rays:
+                out["rays"] = np.zeros((ns, 6), np.float64)
+        o = _RenderOut(*[_addr(out.get(k)) for k in ("rgb8", "rgb_f32", "hit_id", "hit_t", "shadow", "rays",
+                                                     "traversal_stats")])
+        _check(lib().crt_render(self.h, C.byref(cam), C.byref(lt), C.byref(p), C.byref(o), _stream(stream)))
+        return out
+
+
+def render_args(camera, light, width, height, spp, rows=None):
+    cam = _Camera(camera.fov, camera.focal_point, camera.fstop, (C.c_double * 3)(*camera.eye))
+    lt = _Light((C.c_double * 3)(*light.color), (C.c_double * 3)(*light.position), light.radius,
+                light.constant_term, light.linear_term, light.quadratic_term)
+    r0, r1 = rows if rows is not None else (0, 0)
+    return cam, lt, _RenderParams(width, height, spp, r0, r1)
+
+
+def morton(verts, vidx, scene_box, codes, stream=None):
+    """crt_morton on device tensors."""
+    _check(lib().crt_morton(_addr(verts), _addr(vidx), int(vidx.shape[0]), _addr(scene_box), _addr(codes),
+                            _stream(stream)))
+
+
+def sort_pairs(keys_in, vals_in, keys_out, vals_out, key_bits=32, stream=None):
+    """crt_sort_pairs on device tensors (stable LSD radix sort)."""
+    _check(lib().crt_sort_pairs(_addr(keys_in), _addr(vals_in), _addr(keys_out), _addr(vals_out),
+                                int(keys_in.shape[0]), key_bits, _stream(stream)))
+
+
+def camera_angle(fov):
+    return math.tan(math.pi * 0.5 * fov / 180.0)

@@ -326,6 +326,8 @@ def load_obj(path: str) -> Mesh:
 
     def read_mtl(fn):
         m = None
+        if not os.path.exists(os.path.join(base, fn)):  # tinyobjloader warns and goes on
+            return
         with open(os.path.join(base, fn)) as f:
             for line in f:
                 t = line.split()

@@ -1,0 +1,468 @@
+// capi.cu -- the C ABI (include/crt.h): scene ownership, argument checks,
+// host/device staging and error reporting around the kernels of build.cu and
+// trace.cu.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/crt.h"
+#include "crt_internal.h"
+
+using namespace crt;
+
+struct crt_scene {
+  MeshBufs m;
+  BuildBufs b;
+  bool built = false;
+  unsigned* counter = nullptr;
+  void* block = nullptr;  // one allocation backing the build arrays
+  size_t block_bytes = 0;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+crt_status fail(crt_status s, const std::string& msg) {
+  g_err = msg;
+  return s;
+}
+
+crt_status cuda_fail(cudaError_t e, const char* what) {
+  cudaGetLastError();
+  return fail(e == cudaErrorMemoryAllocation ? CRT_OOM : CRT_CUDA_ERROR,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CRT_CUDA(call, what)                     \
+  do {                                           \
+    cudaError_t e_ = (call);                     \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+cudaStream_t S(void* s) { return static_cast<cudaStream_t>(s); }
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+DScene dscene(const crt_scene* s) {
+  DScene d;
+  d.ntri = s->m.ntri;
+  d.root = s->m.ntri >= 2 ? 0 : ~0;
+  d.verts = s->m.verts;
+  d.normals = s->m.normals;
+  d.vidx = s->m.vidx;
+  d.nidx = s->m.nidx;
+  d.matid = s->m.matid;
+  d.mats = s->m.mats;
+  d.nodes = s->b.nodes;
+  d.leaves = s->b.leaves;
+  d.g = s->b.g;
+  return d;
+}
+
+// A device view of a caller buffer: the buffer itself when it is device
+// memory, else a stream-ordered temporary that is copied in and/or out.
+struct DevView {
+  void* user = nullptr;
+  void* dev = nullptr;
+  size_t bytes = 0;
+  bool temp = false;
+  cudaError_t open(void* p, size_t n, bool copy_in, cudaStream_t st) {
+    user = p;
+    bytes = n;
+    if (!p || n == 0) return cudaSuccess;
+    if (is_device_ptr(p)) {
+      dev = p;
+      return cudaSuccess;
+    }
+    temp = true;
+    cudaError_t e = cudaMallocAsync(&dev, n, st);
+    if (e != cudaSuccess) return e;
+    if (copy_in) return cudaMemcpyAsync(dev, p, n, cudaMemcpyDefault, st);
+    return cudaSuccess;
+  }
+  cudaError_t close(bool copy_out, cudaStream_t st) {
+    cudaError_t e = cudaSuccess;
+    if (temp) {
+      if (copy_out) e = cudaMemcpyAsync(user, dev, bytes, cudaMemcpyDefault, st);
+      cudaError_t e2 = cudaFreeAsync(dev, st);
+      if (e == cudaSuccess) e = e2;
+      temp = false;
+    }
+    return e;
+  }
+};
+
+crt_status check_globals(crt_scene* s, cudaStream_t st) {
+  CRT_CUDA(cudaStreamSynchronize(st), "synchronize");
+  if (!s->b.g) return CRT_OK;
+  int err = 0;
+  CRT_CUDA(cudaMemcpy(&err, &s->b.g->err, sizeof(int), cudaMemcpyDeviceToHost), "read error flags");
+  if (err & kErrTimeout) return fail(CRT_TIMEOUT, "a radix-sort look-back wait timed out");
+  if (err & kErrStack) return fail(CRT_STACK_OVERFLOW, "a traversal exceeded the 64-entry stack");
+  if (err & kErrNonFinite) return fail(CRT_INVALID_ARG, "non-finite (or |x| > 1e37) vertex coordinate");
+  return CRT_OK;
+}
+
+void free_scene(crt_scene* s) {
+  cudaFree(s->m.verts);
+  cudaFree(s->m.normals);
+  cudaFree(s->m.vidx);
+  cudaFree(s->m.nidx);
+  cudaFree(s->m.matid);
+  cudaFree(s->m.mats);
+  cudaFree(s->block);
+  cudaFree(s->counter);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* crt_last_error_string(void) { return g_err.c_str(); }
+const char* crt_version(void) { return "cuda-rt-gb300 0.1 (sm_103a)"; }
+
+crt_status crt_scene_create(const crt_mesh_desc* d, void* stream, crt_scene** out) {
+  if (!d || !out) return fail(CRT_INVALID_ARG, "null argument");
+  *out = nullptr;
+  const int n = d->num_triangles;
+  if (n < 0 || n > CRT_MAX_TRIANGLES) return fail(CRT_INVALID_ARG, "num_triangles out of range");
+  if (d->num_vertices < 0 || d->num_normals < 0) return fail(CRT_INVALID_ARG, "negative array size");
+  if (n > 0 && (!d->vertices || !d->vertex_indices || d->num_vertices <= 0))
+    return fail(CRT_INVALID_ARG, "triangles need vertices and vertex_indices");
+  if (n > 0 && (!d->normals || d->num_normals <= 0)) return fail(CRT_INVALID_ARG, "normals are required");
+  if (!d->materials || d->num_materials <= 0) return fail(CRT_INVALID_ARG, "at least one material is required");
+  // Index checks when the indices are host memory.
+  if (n > 0 && !is_device_ptr(d->vertex_indices)) {
+    for (int64_t i = 0; i < 3 * (int64_t)n; i++)
+      if (d->vertex_indices[i] < 0 || d->vertex_indices[i] >= d->num_vertices)
+        return fail(CRT_INVALID_ARG, "vertex index out of range");
+    const int32_t* ni = d->normal_indices ? d->normal_indices : d->vertex_indices;
+    if (!is_device_ptr(ni))
+      for (int64_t i = 0; i < 3 * (int64_t)n; i++)
+        if (ni[i] < 0 || ni[i] >= d->num_normals) return fail(CRT_INVALID_ARG, "normal index out of range");
+    if (d->material_ids && !is_device_ptr(d->material_ids))
+      for (int i = 0; i < n; i++)
+        if (d->material_ids[i] < 0 || d->material_ids[i] >= d->num_materials)
+          return fail(CRT_INVALID_ARG, "material id out of range");
+  }
+  cudaStream_t st = S(stream);
+  crt_scene* s = new crt_scene;
+  MeshBufs& m = s->m;
+  m.nv = d->num_vertices;
+  m.nn = d->num_normals;
+  m.ntri = n;
+  m.nmat = d->num_materials;
+  auto bail = [&](cudaError_t e, const char* what) {
+    crt_status r = cuda_fail(e, what);
+    free_scene(s);
+    delete s;
+    return r;
+  };
+  cudaError_t e;
+#define ALLOC(ptr, bytes)                                                 \
+  if ((bytes) > 0 && (e = cudaMalloc(&(ptr), (bytes))) != cudaSuccess) \
+    return bail(e, "cudaMalloc");
+  ALLOC(m.verts, sizeof(float) * 3 * (size_t)m.nv);
+  ALLOC(m.normals, sizeof(float) * 3 * (size_t)m.nn);
+  ALLOC(m.vidx, sizeof(int) * 3 * (size_t)n);
+  ALLOC(m.nidx, sizeof(int) * 3 * (size_t)n);
+  ALLOC(m.matid, sizeof(int) * (size_t)n);
+  ALLOC(m.mats, sizeof(DMat) * (size_t)m.nmat);
+  ALLOC(s->counter, sizeof(unsigned) * 4);
+  // build arrays, one block
+  BuildBufs& b = s->b;
+  b.n = n;
+  const int tiles = sort_tiles(n > 0 ? n : 1);
+  const size_t nn = n > 0 ? 2 * (size_t)n - 1 : 0;
+  size_t off[10], total = 0;
+  const size_t sizes[10] = {4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n, 4 * 3 * (size_t)kRadix,
+                            4 * 3 * (size_t)tiles * kRadix, 4 * nn, 4 * (size_t)(n > 1 ? n - 1 : 1),
+                            sizeof(BNode) * (size_t)(n > 1 ? n - 1 : 1), sizeof(LeafTri) * (size_t)(n > 0 ? n : 1)};
+  for (int i = 0; i < 10; i++) off[i] = total, total += align256(sizes[i]);
+  const size_t goff = total;
+  total += align256(sizeof(SceneGlobals));
+  ALLOC(s->block, total);
+  s->block_bytes = total;
+#undef ALLOC
+  char* base = static_cast<char*>(s->block);
+  b.keys_a = reinterpret_cast<uint32_t*>(base + off[0]);
+  b.keys_b = reinterpret_cast<uint32_t*>(base + off[1]);
+  b.vals_a = reinterpret_cast<uint32_t*>(base + off[2]);
+  b.vals_b = reinterpret_cast<uint32_t*>(base + off[3]);
+  b.hist = reinterpret_cast<uint32_t*>(base + off[4]);
+  b.status = reinterpret_cast<uint32_t*>(base + off[5]);
+  b.parent = reinterpret_cast<int*>(base + off[6]);
+  b.flags = reinterpret_cast<int*>(base + off[7]);
+  b.nodes = reinterpret_cast<BNode*>(base + off[8]);
+  b.leaves = reinterpret_cast<LeafTri*>(base + off[9]);
+  b.g = reinterpret_cast<SceneGlobals*>(base + goff);
+  if ((e = cudaMemsetAsync(b.g, 0, sizeof(SceneGlobals), st)) != cudaSuccess) return bail(e, "memset");
+  if ((e = cudaMemsetAsync(b.flags, 0, sizes[7], st)) != cudaSuccess) return bail(e, "memset");
+  // upload
+  auto up = [&](void* dst, const void* src, size_t bytes) {
+    return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, st) : cudaSuccess;
+  };
+  if ((e = up(m.verts, d->vertices, sizeof(float) * 3 * (size_t)m.nv)) != cudaSuccess) return bail(e, "upload");
+  if ((e = up(m.normals, d->normals, sizeof(float) * 3 * (size_t)m.nn)) != cudaSuccess) return bail(e, "upload");
+  if ((e = up(m.vidx, d->vertex_indices, sizeof(int) * 3 * (size_t)n)) != cudaSuccess) return bail(e, "upload");
+  if ((e = up(m.nidx, d->normal_indices ? d->normal_indices : d->vertex_indices, sizeof(int) * 3 * (size_t)n)) !=
+      cudaSuccess)
+    return bail(e, "upload");
+  if (d->material_ids) {
+    if ((e = up(m.matid, d->material_ids, sizeof(int) * (size_t)n)) != cudaSuccess) return bail(e, "upload");
+  } else if (n > 0 && (e = cudaMemsetAsync(m.matid, 0, sizeof(int) * (size_t)n, st)) != cudaSuccess) {
+    return bail(e, "memset");
+  }
+  static_assert(sizeof(DMat) == sizeof(crt_material), "material layout");
+  if ((e = up(m.mats, d->materials, sizeof(DMat) * (size_t)m.nmat)) != cudaSuccess) return bail(e, "upload");
+  if ((e = launch_build(m, b, st)) != cudaSuccess) return bail(e, "build launch");
+  s->built = true;
+  crt_status r = check_globals(s, st);
+  if (r != CRT_OK) {
+    std::string msg = g_err;
+    free_scene(s);
+    delete s;
+    return fail(r, msg);
+  }
+  *out = s;
+  return CRT_OK;
+}
+
+crt_status crt_scene_destroy(crt_scene* s) {
+  if (!s) return CRT_OK;
+  cudaDeviceSynchronize();
+  free_scene(s);
+  delete s;
+  return CRT_OK;
+}
+
+crt_status crt_scene_set_vertices(crt_scene* s, const float* v, int rebuild, void* stream) {
+  if (!s || (!v && s->m.nv > 0)) return fail(CRT_INVALID_ARG, "null argument");
+  cudaStream_t st = S(stream);
+  if (s->m.nv > 0)
+    CRT_CUDA(cudaMemcpyAsync(s->m.verts, v, sizeof(float) * 3 * (size_t)s->m.nv, cudaMemcpyDefault, st), "upload");
+  if (rebuild || !s->built) {
+    CRT_CUDA(launch_build(s->m, s->b, st), "build launch");
+    s->built = true;
+  } else {
+    CRT_CUDA(launch_refit(s->m, s->b, st), "refit launch");
+  }
+  return CRT_OK;
+}
+
+crt_status crt_bvh_build(crt_scene* s, void* stream) {
+  if (!s) return fail(CRT_INVALID_ARG, "null scene");
+  CRT_CUDA(launch_build(s->m, s->b, S(stream)), "build launch");
+  s->built = true;
+  return CRT_OK;
+}
+
+crt_status crt_bvh_refit(crt_scene* s, void* stream) {
+  if (!s) return fail(CRT_INVALID_ARG, "null scene");
+  if (!s->built) return fail(CRT_NOT_BUILT, "refit needs a built BVH");
+  CRT_CUDA(launch_refit(s->m, s->b, S(stream)), "refit launch");
+  return CRT_OK;
+}
+
+crt_status crt_scene_check(crt_scene* s, void* stream) {
+  if (!s) return fail(CRT_INVALID_ARG, "null scene");
+  return check_globals(s, S(stream));
+}
+
+crt_status crt_bvh_export(crt_scene* s, float* scene_box, int32_t* codes, uint32_t* ids, int32_t* nodes3,
+                          float* node_boxes, void* stream) {
+  if (!s) return fail(CRT_INVALID_ARG, "null scene");
+  if (!s->built) return fail(CRT_NOT_BUILT, "no BVH");
+  cudaStream_t st = S(stream);
+  CRT_CUDA(cudaStreamSynchronize(st), "synchronize");
+  const int n = s->m.ntri;
+  const size_t nn = n > 0 ? 2 * (size_t)n - 1 : 0;
+  SceneGlobals g;
+  CRT_CUDA(cudaMemcpy(&g, s->b.g, sizeof(g), cudaMemcpyDeviceToHost), "download");
+  auto ord2f_h = [](int i) {
+    int bits = i >= 0 ? i : i ^ 0x7FFFFFFF;
+    float f;
+    std::memcpy(&f, &bits, 4);
+    return f;
+  };
+  std::vector<float> box(6);
+  for (int k = 0; k < 3; k++) box[k] = ord2f_h(g.bmin[k]), box[3 + k] = ord2f_h(g.bmax[k]);
+  std::vector<uint32_t> hk(n), hv(n);
+  std::vector<int> parent(nn);
+  std::vector<BNode> nodes(n > 1 ? n - 1 : 0);
+  if (n > 0) {
+    CRT_CUDA(cudaMemcpy(hk.data(), s->b.keys_b, 4 * (size_t)n, cudaMemcpyDeviceToHost), "download");
+    CRT_CUDA(cudaMemcpy(hv.data(), s->b.vals_b, 4 * (size_t)n, cudaMemcpyDeviceToHost), "download");
+    CRT_CUDA(cudaMemcpy(parent.data(), s->b.parent, 4 * nn, cudaMemcpyDeviceToHost), "download");
+  }
+  if (n > 1) CRT_CUDA(cudaMemcpy(nodes.data(), s->b.nodes, sizeof(BNode) * (n - 1), cudaMemcpyDeviceToHost), "download");
+  std::vector<int> n3(3 * nn);
+  std::vector<float> nb(6 * nn);
+  auto ref = [n](int code) { return code >= 0 ? code : (n - 1) + ~code; };
+  for (size_t i = 0; i < nn; i++) n3[3 * i] = (i == 0) ? -1 : parent[i];
+  for (int k = 0; k < n; k++) {
+    n3[3 * ((n - 1) + k) + 1] = (int)hv[k];
+    n3[3 * ((n - 1) + k) + 2] = (int)hv[k];
+  }
+  for (int i = 0; i < n - 1; i++) {
+    const BNode& b = nodes[i];
+    const int l = ref(b.child.x), r = ref(b.child.y);
+    n3[3 * i + 1] = l;
+    n3[3 * i + 2] = r;
+    const float lb[6] = {b.xy_l.x, b.xy_l.z, b.z_lr.x, b.xy_l.y, b.xy_l.w, b.z_lr.y};
+    const float rbx[6] = {b.xy_r.x, b.xy_r.z, b.z_lr.z, b.xy_r.y, b.xy_r.w, b.z_lr.w};
+    std::memcpy(&nb[6 * (size_t)l], lb, sizeof(lb));
+    std::memcpy(&nb[6 * (size_t)r], rbx, sizeof(rbx));
+  }
+  if (nn > 0) std::memcpy(&nb[0], g.root_box, 6 * sizeof(float));
+  auto put = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+    if (!dst || !bytes) return cudaSuccess;
+    return cudaMemcpy(dst, src, bytes, cudaMemcpyDefault);
+  };
+  CRT_CUDA(put(scene_box, box.data(), 6 * sizeof(float)), "export");
+  CRT_CUDA(put(codes, hk.data(), 4 * (size_t)n), "export");
+  CRT_CUDA(put(ids, hv.data(), 4 * (size_t)n), "export");
+  CRT_CUDA(put(nodes3, n3.data(), 4 * n3.size()), "export");
+  CRT_CUDA(put(node_boxes, nb.data(), 4 * nb.size()), "export");
+  return CRT_OK;
+}
+
+static crt_status trace_common(crt_scene* s, const double* rays, int64_t n, int32_t* ids, double* t,
+                               double* normals, bool any, void* stream) {
+  if (!s || n < 0 || (n > 0 && (!rays || !ids))) return fail(CRT_INVALID_ARG, "bad trace arguments");
+  if (!s->built) return fail(CRT_NOT_BUILT, "no BVH");
+  if (n == 0) return CRT_OK;
+  cudaStream_t st = S(stream);
+  DevView vr, vi, vt, vn;
+  CRT_CUDA(vr.open(const_cast<double*>(rays), 6 * sizeof(double) * (size_t)n, true, st), "stage rays");
+  CRT_CUDA(vi.open(ids, sizeof(int32_t) * (size_t)n, false, st), "stage ids");
+  CRT_CUDA(vt.open(t, sizeof(double) * (size_t)n, false, st), "stage t");
+  CRT_CUDA(vn.open(any ? nullptr : normals, 3 * sizeof(double) * (size_t)n, false, st), "stage normals");
+  CRT_CUDA(launch_trace(dscene(s), static_cast<const double*>(vr.dev), n, any, static_cast<int*>(vi.dev),
+                        static_cast<double*>(vt.dev), static_cast<double*>(vn.dev), st),
+           "trace launch");
+  const bool host_out = vi.temp || vt.temp || vn.temp;
+  CRT_CUDA(vr.close(false, st), "unstage");
+  CRT_CUDA(vi.close(true, st), "unstage");
+  CRT_CUDA(vt.close(true, st), "unstage");
+  CRT_CUDA(vn.close(true, st), "unstage");
+  if (host_out) return check_globals(s, st);
+  return CRT_OK;
+}
+
+crt_status crt_trace_closest(crt_scene* s, const double* rays, int64_t n, int32_t* ids, double* t, double* normals,
+                             void* stream) {
+  return trace_common(s, rays, n, ids, t, normals, false, stream);
+}
+
+crt_status crt_trace_shadow(crt_scene* s, const double* rays, int64_t n, int32_t* ids, double* t, void* stream) {
+  return trace_common(s, rays, n, ids, t, nullptr, true, stream);
+}
+
+crt_status crt_render(crt_scene* s, const crt_camera* cam, const crt_light* light, const crt_render_params* p,
+                      const crt_render_out* o, void* stream) {
+  if (!s || !cam || !light || !p || !o) return fail(CRT_INVALID_ARG, "null argument");
+  if (!s->built) return fail(CRT_NOT_BUILT, "no BVH");
+  if (p->width <= 0 || p->height <= 0 || p->spp <= 0) return fail(CRT_INVALID_ARG, "width, height, spp must be > 0");
+  if ((int64_t)p->width * p->height > (int64_t)1 << 30) return fail(CRT_INVALID_ARG, "image too large");
+  int row0 = p->row_begin, row1 = p->row_end;
+  if (row0 == 0 && row1 == 0) row1 = p->height;
+  if (row0 < 0 || row1 > p->height || row0 >= row1) return fail(CRT_INVALID_ARG, "bad row range");
+  cudaStream_t st = S(stream);
+  const size_t npx = (size_t)p->width * p->height;
+  const size_t nsm = npx * (size_t)p->spp;
+  RenderArgs a;
+  a.W = p->width, a.H = p->height, a.spp = p->spp, a.row0 = row0, a.row1 = row1;
+  // the constants of raytracer.cu:126-130, 144; tan on the host
+  a.angle = std::tan(M_PI * 0.5 * cam->fov / 180.0f);
+  a.aspect = double(p->width) / double(p->height);
+  a.invW = 1.0 / double(p->width);
+  a.invH = 1.0 / double(p->height);
+  a.aperture = 1 / cam->fstop;
+  a.focal = cam->focal_point;
+  for (int k = 0; k < 3; k++) {
+    a.eye[k] = cam->eye[k];
+    a.lpos[k] = light->position[k];
+    a.lcol[k] = light->color[k];
+  }
+  a.lradius = light->radius;
+  a.latt[0] = light->constant_term, a.latt[1] = light->linear_term, a.latt[2] = light->quadratic_term;
+  a.counter = s->counter;
+  // outputs: whole-image buffers; a row band writes only its rows
+  DevView v8, vf, vh, vt, vs, vr, vst;
+  const bool band = !(row0 == 0 && row1 == p->height);
+  CRT_CUDA(v8.open(o->rgb8, 3 * npx, band, st), "stage rgb8");
+  CRT_CUDA(vf.open(o->rgb_f32, 3 * sizeof(float) * npx, band, st), "stage rgb_f32");
+  CRT_CUDA(vh.open(o->hit_id, sizeof(int32_t) * nsm, band, st), "stage hit_id");
+  CRT_CUDA(vt.open(o->hit_t, sizeof(double) * nsm, band, st), "stage hit_t");
+  CRT_CUDA(vs.open(o->shadow, sizeof(int32_t) * nsm, band, st), "stage shadow");
+  CRT_CUDA(vr.open(o->rays, 6 * sizeof(double) * nsm, band, st), "stage rays");
+  CRT_CUDA(vst.open(o->traversal_stats, 2 * sizeof(uint64_t), false, st), "stage stats");
+  if (vst.dev) CRT_CUDA(cudaMemsetAsync(vst.dev, 0, 2 * sizeof(uint64_t), st), "memset");
+  a.rgb8 = static_cast<uint8_t*>(v8.dev);
+  a.rgbf = static_cast<float*>(vf.dev);
+  a.hit_id = static_cast<int*>(vh.dev);
+  a.hit_t = static_cast<double*>(vt.dev);
+  a.shadow = static_cast<int*>(vs.dev);
+  a.rays = static_cast<double*>(vr.dev);
+  a.stats = static_cast<unsigned long long*>(vst.dev);
+  CRT_CUDA(launch_render(dscene(s), a, st), "render launch");
+  const bool host_out = v8.temp || vf.temp || vh.temp || vt.temp || vs.temp || vr.temp || vst.temp;
+  CRT_CUDA(v8.close(true, st), "unstage");
+  CRT_CUDA(vf.close(true, st), "unstage");
+  CRT_CUDA(vh.close(true, st), "unstage");
+  CRT_CUDA(vt.close(true, st), "unstage");
+  CRT_CUDA(vs.close(true, st), "unstage");
+  CRT_CUDA(vr.close(true, st), "unstage");
+  CRT_CUDA(vst.close(true, st), "unstage");
+  if (host_out) return check_globals(s, st);
+  return CRT_OK;
+}
+
+crt_status crt_morton(const float* verts, const int32_t* vidx, int32_t n, const float* box6, int32_t* codes,
+                      void* stream) {
+  if (n < 0 || (n > 0 && (!verts || !vidx || !box6 || !codes))) return fail(CRT_INVALID_ARG, "bad arguments");
+  if (n > 0 && !(is_device_ptr(verts) && is_device_ptr(vidx) && is_device_ptr(box6) && is_device_ptr(codes)))
+    return fail(CRT_INVALID_ARG, "crt_morton takes device pointers");
+  CRT_CUDA(launch_morton(verts, vidx, n, box6, reinterpret_cast<uint32_t*>(codes), S(stream)), "morton launch");
+  return CRT_OK;
+}
+
+crt_status crt_sort_pairs(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, int32_t n,
+                          int32_t key_bits, void* stream) {
+  if (n < 0 || n > CRT_MAX_TRIANGLES || key_bits < 1 || key_bits > 32) return fail(CRT_INVALID_ARG, "bad sizes");
+  if (n == 0) return CRT_OK;
+  if (!kin || !kout || !vout) return fail(CRT_INVALID_ARG, "null array");
+  if (!(is_device_ptr(kin) && is_device_ptr(kout) && is_device_ptr(vout) && (!vin || is_device_ptr(vin))))
+    return fail(CRT_INVALID_ARG, "crt_sort_pairs takes device pointers");
+  cudaStream_t st = S(stream);
+  const size_t bytes = sort_scratch_bytes(n, key_bits) + 256;
+  void* scratch = nullptr;
+  CRT_CUDA(cudaMallocAsync(&scratch, bytes, st), "scratch");
+  int* err = reinterpret_cast<int*>(static_cast<char*>(scratch) + bytes - 256);
+  cudaError_t e = cudaMemsetAsync(err, 0, sizeof(int), st);
+  if (e == cudaSuccess) e = launch_sort_pairs(kin, vin, kout, vout, n, key_bits, scratch, err, st);
+  int herr = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaError_t e2 = cudaFreeAsync(scratch, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) return cuda_fail(e, "sort");
+  if (herr & kErrTimeout) return fail(CRT_TIMEOUT, "a radix-sort look-back wait timed out");
+  return CRT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,76 @@
+// crt_internal.h -- host-side interfaces between the library's translation
+// units (build.cu, trace.cu, capi.cu).  Not part of the public ABI.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "crt_device.cuh"
+
+namespace crt {
+
+// Sort geometry shared by the build and the standalone sort.
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;
+constexpr int kRadixBits = 10;
+constexpr int kRadix = 1 << kRadixBits;
+
+inline int sort_passes(int key_bits) { return (key_bits + kRadixBits - 1) / kRadixBits; }
+inline int sort_tiles(int n) { return (n + kSortTile - 1) / kSortTile; }
+
+// Device arrays of one scene's BVH build (owned by the scene).
+struct BuildBufs {
+  int n = 0;
+  uint32_t *keys_a = nullptr, *keys_b = nullptr, *vals_a = nullptr, *vals_b = nullptr;
+  uint32_t* hist = nullptr;    // 3 * kRadix
+  uint32_t* status = nullptr;  // 3 * tiles * kRadix
+  int* parent = nullptr;       // 2n - 1, reference numbering
+  int* flags = nullptr;        // n - 1
+  BNode* nodes = nullptr;      // n - 1
+  LeafTri* leaves = nullptr;   // n
+  SceneGlobals* g = nullptr;
+};
+
+// Mesh arrays on the device.
+struct MeshBufs {
+  int nv = 0, nn = 0, ntri = 0, nmat = 0;
+  float* verts = nullptr;
+  float* normals = nullptr;
+  int* vidx = nullptr;
+  int* nidx = nullptr;
+  int* matid = nullptr;
+  DMat* mats = nullptr;
+};
+
+int num_sms();
+
+// build.cu
+cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st);
+cudaError_t launch_refit(const MeshBufs& m, const BuildBufs& b, cudaStream_t st);
+cudaError_t launch_morton(const float* verts, const int* vidx, int n, const float* box6, uint32_t* codes,
+                          cudaStream_t st);
+// Stable LSD radix sort; scratch holds sort_scratch_bytes(n, key_bits).
+size_t sort_scratch_bytes(int n, int key_bits);
+cudaError_t launch_sort_pairs(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, int n,
+                              int key_bits, void* scratch, int* err, cudaStream_t st);
+
+// trace.cu
+struct RenderArgs {
+  int W, H, spp, row0, row1;
+  double angle, aspect, invW, invH, aperture, focal;
+  double eye[3];
+  double lpos[3], lcol[3], lradius, latt[3];
+  uint8_t* rgb8;
+  float* rgbf;
+  int* hit_id;
+  double* hit_t;
+  int* shadow;
+  double* rays;
+  unsigned* counter;
+  unsigned long long* stats;  // optional [2]: internal nodes visited, triangles tested
+};
+cudaError_t launch_render(const DScene& S, const RenderArgs& a, cudaStream_t st);
+cudaError_t launch_trace(const DScene& S, const double* rays, int64_t n, bool any, int* ids, double* t,
+                         double* normals, cudaStream_t st);
+
+}  // namespace crt

@@ -1,0 +1,179 @@
+/* crt.h -- C ABI of the GB300-native cuda-rt ray-tracing hot path.
+ *
+ * One shared library (libcrt.so) built for sm_103a.  Plain pointers and
+ * sizes only.  Unless a comment says otherwise, every pointer argument may
+ * be host memory (pageable or pinned) or device memory; the library checks
+ * which (cudaPointerGetAttributes) and copies as needed.  Calls that take a
+ * `stream` are ordered on it (NULL = legacy default stream); calls that read
+ * results into host memory synchronise that stream before returning.
+ *
+ * Every entry point returns a crt_status and never exits the process
+ * (the reference prints and calls exit(1): src/scene.cpp:71-81).
+ * crt_last_error_string() describes the last failure on the calling thread.
+ *
+ * Semantics follow the reference (mbartling/cuda-rt) bit for bit; each
+ * declaration names the reference interface it replaces.
+ */
+#ifndef CRT_H_
+#define CRT_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum crt_status {
+  CRT_OK = 0,
+  CRT_INVALID_ARG = 1,
+  CRT_OOM = 2,
+  CRT_CUDA_ERROR = 3,
+  CRT_STACK_OVERFLOW = 4, /* a traversal needed more than 64 stack entries */
+  CRT_TIMEOUT = 5,        /* a bounded device-side wait gave up */
+  CRT_NOT_BUILT = 6,      /* the scene has no BVH yet */
+} crt_status;
+
+/* Largest triangle count one scene accepts.  It keeps every radix-tree depth
+ * below 62, so the reference's 64-entry traversal stack (kernels/bvh.cu:379)
+ * can never overflow. */
+#define CRT_MAX_TRIANGLES (1 << 28)
+
+typedef struct crt_scene crt_scene;
+
+/* Material, inc/material.h:8-24: the fields Material::shade and
+ * Light::shadowAttenuation read.  Trans() is isZero(kt), as in the
+ * reference (inc/material.h:31). */
+typedef struct crt_material {
+  double ka[3], kd[3], ks[3], kt[3], ke[3];
+  double shininess;
+} crt_material;
+
+/* A triangle mesh in FP32, indexed.  Replaces Scene_h (inc/scene.h:29-56):
+ * vertices/normals are tinyobj's attrib_t arrays, the index arrays are
+ * TriangleIndices' vertex_index / normal_index (inc/tris.h:9-13).
+ * normal_indices may be NULL (then vertex_indices index the normals too);
+ * material_ids may be NULL (every triangle uses material 0). */
+typedef struct crt_mesh_desc {
+  const float* vertices;   /* num_vertices * 3 */
+  int32_t num_vertices;
+  const float* normals;    /* num_normals * 3 */
+  int32_t num_normals;
+  const int32_t* vertex_indices; /* num_triangles * 3 */
+  const int32_t* normal_indices; /* num_triangles * 3 or NULL */
+  int32_t num_triangles;
+  const crt_material* materials; /* num_materials */
+  int32_t num_materials;
+  const int32_t* material_ids;   /* num_triangles or NULL */
+} crt_mesh_desc;
+
+/* The Camera getters the pixel kernel reads (inc/camera.h:26-40):
+ * setfov (vertical, degrees), setFocalPoint, setFstop (aperture = 1/fstop;
+ * INFINITY gives a pinhole).  eye is Camera::getEye, read only by the
+ * specular term.  As in the reference, the camera sits at the origin and
+ * looks down -z (kernels/raytracer.cu:126-154). */
+typedef struct crt_camera {
+  double fov;
+  double focal_point;
+  double fstop;
+  double eye[3];
+} crt_camera;
+
+/* Light_h, inc/Light.h:7-29 (positional light; orientation unused). */
+typedef struct crt_light {
+  double color[3];
+  double position[3];
+  double radius;
+  double constant_term, linear_term, quadratic_term;
+} crt_light;
+
+typedef struct crt_render_params {
+  int32_t width, height;
+  int32_t spp;                 /* samples per pixel (the reference fixes 20: raytracer.cu:138) */
+  int32_t row_begin, row_end;  /* rows [begin, end) counted from the top; 0,0 = all */
+} crt_render_params;
+
+/* Outputs of crt_render.  Pixel (px, py), py counted from the top, is stored
+ * at idx = (height - py - 1) * width + px, the reference's bottom-up order
+ * (kernels/raytracer.cu:106).  Any pointer may be NULL. */
+typedef struct crt_render_out {
+  uint8_t* rgb8;     /* idx*3: (unsigned char)(255 * clamp(mean colour)) */
+  float* rgb_f32;    /* idx*3: mean colour before clamping */
+  int32_t* hit_id;   /* idx*spp + k: closest-hit triangle of sample k, -1 miss */
+  double* hit_t;     /* idx*spp + k: its t */
+  int32_t* shadow;   /* idx*spp + k: 1 occluded, 0 lit, -1 primary miss */
+  double* rays;      /* (idx*spp + k)*6: primary ray origin, direction */
+  uint64_t* traversal_stats; /* [2]: internal nodes visited, triangles tested (all
+                                rays of the call); non-NULL selects an instrumented kernel */
+} crt_render_out;
+
+/* ---- scene lifetime: Scene_d::operator=(const Scene_h&) (src/scene.cpp:82-160)
+ * uploads the mesh and builds the BVH; ~Scene_d (src/scene.cpp:163-171) frees.
+ * crt_scene_create does both steps and synchronises `stream`. */
+crt_status crt_scene_create(const crt_mesh_desc* mesh, void* stream, crt_scene** out);
+crt_status crt_scene_destroy(crt_scene* scene);
+
+/* New vertex positions for the same triangles (num_vertices * 3 floats),
+ * then either a full LBVH rebuild (rebuild != 0) or an atomic bottom-up
+ * refit on the existing topology (RefitBounds, kernels/bvh.cu:209-258).
+ * Asynchronous on `stream`. */
+crt_status crt_scene_set_vertices(crt_scene* scene, const float* vertices, int rebuild, void* stream);
+
+/* ---- BVH: BVH_d::setUp / computeMortonCodes / sortMortonCodes / buildTree
+ * (src/bvh.cpp:3-32, kernels/bvh.cu:260-292).  Asynchronous. */
+crt_status crt_bvh_build(crt_scene* scene, void* stream);
+/* RefitBounds on the current topology after the vertices changed in place. */
+crt_status crt_bvh_refit(crt_scene* scene, void* stream);
+
+/* Copies the build products in the reference's layout (inc/bvh.cuh:18-28):
+ * nodes 0..N-2 internal, N-1..2N-2 leaves.  Host or device pointers, any
+ * may be NULL; synchronises `stream`.
+ *   scene_box[6]           findMinMax's mMin, mMax (kernels/scene.cu:72-85)
+ *   codes[N], ids[N]       mortonCodes / object_ids after the sort
+ *   nodes3[(2N-1)*3]       HNode parent, left, right (root parent = -1)
+ *   node_boxes[(2N-1)*6]   sortedBBoxs lo xyz, hi xyz */
+crt_status crt_bvh_export(crt_scene* scene, float* scene_box, int32_t* codes, uint32_t* ids, int32_t* nodes3,
+                          float* node_boxes, void* stream);
+
+/* ---- traversal: BVH_d::intersect (closest hit, kernels/bvh.cu:382-414)
+ * and BVH_d::intersectAny (first hit in left-first DFS order,
+ * kernels/bvh.cu:416-449).  rays: n * 6 doubles (origin, direction).
+ * ids[n]: triangle id or -1; t[n]; normals[n*3] (closest only; the
+ * smooth normal of bvh.cu:357-364).  t and normals may be NULL. */
+crt_status crt_trace_closest(crt_scene* scene, const double* rays, int64_t n, int32_t* ids, double* t,
+                             double* normals, void* stream);
+crt_status crt_trace_shadow(crt_scene* scene, const double* rays, int64_t n, int32_t* ids, double* t,
+                            void* stream);
+
+/* ---- render: RayTracer::run + pullRaytracedImage (kernels/raytracer.cu:55-166,
+ * inc/raytracer.h:53-63): thin-lens primary rays on the mrand stream,
+ * closest hit, Material::shade with one shadow ray per hit, mean over the
+ * samples, clamp, quantise. */
+crt_status crt_render(crt_scene* scene, const crt_camera* camera, const crt_light* light,
+                      const crt_render_params* params, const crt_render_out* out, void* stream);
+
+/* ---- stage-level entry points (device pointers only, asynchronous) ----
+ * Morton codes of each triangle's centroid (computeMortonCodesKernel,
+ * kernels/bvh.cu:37-61), normalised by scene_box (6 floats, device). */
+crt_status crt_morton(const float* vertices, const int32_t* vertex_indices, int32_t num_triangles,
+                      const float* scene_box, int32_t* codes, void* stream);
+/* Stable ascending LSD radix sort of (key, value) pairs on the low
+ * `key_bits` bits of the keys (thrust::sort_by_key, kernels/bvh.cu:267-273).
+ * vals_in may be NULL: values are then 0..n-1.  In and out arrays must not
+ * overlap.  Scratch is allocated per call (cudaMallocAsync); the call
+ * synchronises `stream` and reports a look-back timeout as CRT_TIMEOUT. */
+crt_status crt_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
+                          int32_t n, int32_t key_bits, void* stream);
+
+/* Synchronise `stream` and report device-side errors the scene's kernels
+ * recorded (stack overflow, bounded-wait timeout, non-finite input). */
+crt_status crt_scene_check(crt_scene* scene, void* stream);
+
+const char* crt_last_error_string(void);
+const char* crt_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CRT_H_ */

@@ -1,0 +1,110 @@
+"""LBVH build on the GPU: bit-exact against the reference (golden fixtures)
+and against the oracle on fresh seeded scenes, through the C ABI."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import assert_equal, golden_files, golden_mesh
+
+pytestmark = pytest.mark.gpu
+
+
+def _build_equal(gpu_ex, ref, tri_boxes=None):
+    for k in ("codes", "ids", "nodes", "node_boxes"):
+        assert_equal(gpu_ex[k], ref[k], k)
+    box = np.concatenate([ref["smin"], ref["smax"]]).astype(np.float32)
+    assert_equal(gpu_ex["scene_box"], box, "scene box")
+
+
+@pytest.mark.parametrize("path", golden_files(), ids=lambda p: os.path.basename(p)[:-4])
+def test_build_matches_reference_golden(cuda, path):
+    import crt
+    z = np.load(path)
+    s = crt.Scene(golden_mesh(z))
+    _build_equal(s.export(), z)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 31, 2047, 2048, 2049, 100_000])
+def test_build_matches_oracle_soup(cuda, n):
+    import crt
+    from crt import data
+    from oracle.oracle import OracleScene
+    m = data.soup(n, seed=n)
+    _build_equal(crt.Scene(m).export(), OracleScene(m).export())
+
+
+def test_build_matches_oracle_icosphere_1m(cuda):
+    import crt
+    from crt import data
+    from oracle.oracle import OracleScene
+    m = data.icosphere(224)
+    _build_equal(crt.Scene(m).export(), OracleScene(m).export())
+
+
+def test_build_duplicate_codes(cuda):
+    """Runs of equal Morton codes exercise delta()'s index tie-break."""
+    import crt
+    from crt import data
+    from oracle.oracle import OracleScene
+    rng = np.random.default_rng(1)
+    n = 20000
+    cent = rng.integers(0, 3, (n, 3)).astype(np.float64)
+    off = rng.normal(0, 1e-4, (n, 3, 3))
+    off -= off.mean(1, keepdims=True)
+    v = (cent[:, None, :] + off).reshape(-1, 3).astype(np.float32)
+    vidx = np.arange(3 * n, dtype=np.int32).reshape(n, 3)
+    nrm = np.tile(np.array([[0, 0, 1]], np.float32), (3 * n, 1))
+    m = data.Mesh(v, vidx, nrm, vidx.copy(), np.zeros(n, np.int32), data.lambert_material()[None])
+    _build_equal(crt.Scene(m).export(), OracleScene(m).export())
+
+
+def test_rebuild_is_idempotent(cuda):
+    import crt
+    from crt import data
+    m = data.soup(5000, seed=3)
+    s = crt.Scene(m)
+    a = s.export()
+    s.build()
+    b = s.export()
+    for k in a:
+        assert_equal(a[k], b[k], k)
+
+
+@pytest.mark.parametrize("n,bits", [(1, 30), (5, 30), (2048, 30), (2049, 30), (300_000, 30), (300_000, 32),
+                                    (100_000, 10), (70_000, 17)])
+def test_sort_pairs_stable(cuda, n, bits):
+    import crt
+    torch = cuda
+    rng = np.random.default_rng(n + bits)
+    hi = min(1 << bits, 1 << 32)
+    keys = rng.integers(0, hi, n, dtype=np.uint64).astype(np.uint32)
+    keys[: n // 3] = keys[0]  # a long run of equal keys tests stability
+    rng.shuffle(keys)
+    vals = rng.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32)
+    kin = torch.from_numpy(keys.view(np.int32)).cuda()
+    vin = torch.from_numpy(vals.view(np.int32)).cuda()
+    ko, vo = torch.empty_like(kin), torch.empty_like(vin)
+    crt.sort_pairs(kin, vin, ko, vo, key_bits=bits)
+    order = np.argsort(keys, kind="stable")
+    assert_equal(ko.cpu().numpy().view(np.uint32), keys[order], "keys")
+    assert_equal(vo.cpu().numpy().view(np.uint32), vals[order], "values")
+    # values omitted: indices 0..n-1
+    crt.sort_pairs(kin, None, ko, vo, key_bits=bits)
+    assert_equal(vo.cpu().numpy(), order.astype(np.int32), "implicit values")
+
+
+def test_morton_stage_matches_oracle(cuda):
+    import crt
+    from crt import data
+    from oracle.oracle import OracleScene
+    torch = cuda
+    m = data.soup(50_000, seed=11)
+    ex = OracleScene(m).export()
+    box = torch.tensor(np.concatenate([ex["smin"], ex["smax"]]).astype(np.float32)).cuda()
+    v = torch.from_numpy(m.verts).cuda()
+    vi = torch.from_numpy(m.vidx).cuda()
+    codes = torch.empty(m.ntri, dtype=torch.int32, device="cuda")
+    crt.morton(v, vi, box, codes)
+    torch.cuda.synchronize()
+    assert_equal(codes.cpu().numpy(), ex["codes_unsorted"], "codes")
