@@ -34,11 +34,14 @@ __device__ __forceinline__ void tri_box(const float* __restrict__ V, const int* 
   lo[2] = fminf(c.z, fminf(a.z, b.z)), hi[2] = fmaxf(c.z, fmaxf(a.z, b.z));
 }
 
-__device__ __forceinline__ bool finite_coords(float lo[3], float hi[3]) {
-  bool ok = true;
-#pragma unroll
-  for (int k = 0; k < 3; k++) ok = ok && fabsf(lo[k]) <= 1e37f && fabsf(hi[k]) <= 1e37f;
-  return ok;
+// Every coordinate finite and |x| <= 1e37 (fminf/fmaxf would hide a NaN
+// inside the box, so the vertices themselves are checked).
+__device__ __forceinline__ bool finite_coords(float3 a, float3 b, float3 c) {
+  const float m = fmaxf(fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fmaxf(fabsf(a.z), fabsf(b.x))),
+                        fmaxf(fmaxf(fabsf(b.y), fabsf(b.z)), fmaxf(fmaxf(fabsf(c.x), fabsf(c.y)), fabsf(c.z))));
+  const bool nan = (a.x != a.x) | (a.y != a.y) | (a.z != a.z) | (b.x != b.x) | (b.y != b.y) | (b.z != b.z) |
+                   (c.x != c.x) | (c.y != c.y) | (c.z != c.z);
+  return !nan && m <= 1e37f;
 }
 
 __global__ void k_build_init(SceneGlobals* g, uint32_t* hist, int nhist) {
@@ -64,7 +67,7 @@ __global__ void __launch_bounds__(256) k_bounds(const float* __restrict__ V, con
     float3 a, b, c;
     float l[3], h[3];
     tri_box(V, vidx, t, a, b, c, l, h);
-    ok = ok && finite_coords(l, h);
+    ok = ok && finite_coords(a, b, c);
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       lo[k] = fminf(lo[k], l[k]);
@@ -423,7 +426,7 @@ __global__ void __launch_bounds__(256) k_refit(const float* __restrict__ V, cons
     float3 a, b, c;
     float lo[3], hi[3];
     tri_box(V, vidx, tri, a, b, c, lo, hi);
-    ok = finite_coords(lo, hi);
+    ok = finite_coords(a, b, c);
     e = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
     LeafTri lt;
     lt.v0 = make_float4(a.x, a.y, a.z, __int_as_float(tri));

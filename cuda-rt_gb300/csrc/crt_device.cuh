@@ -97,135 +97,221 @@ __device__ __forceinline__ double norm_exact(D3 a) {
 }
 
 // ---------------------------------------------------------------- rays
-// Per-ray constants: the double ray for the exact tests, and an FP32 copy
-// with error margins for the conservative box filter.
+// Per-ray constants: the double ray for the exact tests, and an FP32 form
+// whose rounding is bounded, for filters that decide most tests without
+// any double arithmetic.
 struct RayC {
   double ox, oy, oz, dx, dy, dz;
-  double ix, iy, iz;     // 1.0/d, as bbox.h:88 computes it
-  float fox, foy, foz;   // origin rounded to float
-  float fix, fiy, fiz;   // 1/d rounded to float; 0 on a "free" axis
-  float mx, my, mz;      // accept margins (t units); +inf on a free axis
-  float px, py, pz;      // prune margins: accept margin + box dilation
+  float fox, foy, foz, fdx, fdy, fdz;  // origin, direction rounded to float
+  float omax;            // max |origin| component (float, rounded up)
+  float ax, ay, az;      // 1/d in float; 0 on a "free" axis
+  float lx, ly, lz;      // RD(c - m), c = RN(-o_f * a_f)
+  float hx, hy, hz;      // RU(c + m)
+  float dprune;          // widening of the entry bound for pruning
   float tau;             // slack on t for pruning
+  int sx, sy, sz;        // 1 when 1/d < 0: the box's hi plane is the near one
 };
 
-// Conservative-filter bounds (derivation in the design notes):
-//  |t_f32 - t_f64| <= 4.01 u |a| (|b| + |e|), u = 2^-24, for a slab value
-//  t = (b - e) * a; the margin uses 8u (a factor 2 of headroom) and B >= |b|.
-//  Pruning a subtree is safe when its dilated-box entry bound exceeds the
-//  best t by tau; eps bounds how far a double Moller-Trumbore hit can fall
-//  outside its triangle (alpha/beta rounding) and tau how far its t can be
-//  off (see prune_ok).  Both carry a 2^23 factor of headroom over a
-//  first-order rounding analysis with |det| >= 1e-8.
+// Slab filter constants.  For a box coordinate b (a float) the exact test
+// uses t = (b - o) * a in double, a = 1.0/d.  Here, in float,
+//   a_f = RN(1/RN(d)), c = RN(-RN(o) * a_f),
+//   |b a_f + c - t| <= 4.1 u |a| (|b| + |o|)      (u = 2^-24),
+// and the margin is m = 8 u |a_f| (B + |o_f|), B >= |b| over the scene.  So
+//   RD(b a_f + RD(c - m)) <= t <= RU(b a_f + RU(c + m))
+// for every slab value the exact test can produce.  An axis whose constants
+// do not fit comfortably in float ("free") never decides anything.
+//
+// Pruning (closest hit only): a triangle the exact test accepts may put its
+// plane crossing up to eps outside the triangle (alpha/beta rounding) and its
+// t up to tau away from that crossing; eps and tau bound first-order rounding
+// of Moller-Trumbore with |det| >= 1e-8 for triangles of diameter <= D, with
+// a factor 2^23 of headroom.  A subtree whose entry bound, lowered by
+// dprune = eps * max|a|, exceeds best + tau cannot hold a t <= best.
 __device__ __forceinline__ void ray_setup(RayC& r, double ox, double oy, double oz, double dx, double dy, double dz,
                                           float B, float D) {
   r.ox = ox, r.oy = oy, r.oz = oz, r.dx = dx, r.dy = dy, r.dz = dz;
-  r.ix = 1.0 / dx, r.iy = 1.0 / dy, r.iz = 1.0 / dz;
-  const double omax = fmax(fmax(fabs(ox), fabs(oy)), fabs(oz));
-  const double Dd = (double)D;
-  const double reach = 1.7320508075688772 * (omax + (double)B);
-  const double eps = 1.862645149230957e-09 * Dd * Dd * (reach + Dd) / 1e-8;          // 2^-29
-  const double tau = 9.313225746154785e-10 * Dd * Dd * (4.0 * reach + Dd) / 1e-8;    // 2^-30
-  r.tau = __double2float_ru(tau);
-  double o[3] = {ox, oy, oz}, a[3] = {r.ix, r.iy, r.iz};
-  float fo[3], fi[3], m[3], p[3];
+  const float fo[3] = {__double2float_rn(ox), __double2float_rn(oy), __double2float_rn(oz)};
+  const float fd[3] = {__double2float_rn(dx), __double2float_rn(dy), __double2float_rn(dz)};
+  r.fox = fo[0], r.foy = fo[1], r.foz = fo[2];
+  r.fdx = fd[0], r.fdy = fd[1], r.fdz = fd[2];
+  // |o| rounded up: float rounding of o is at most a relative 2^-24
+  const float omax = __fmul_ru(fmaxf(fmaxf(fabsf(fo[0]), fabsf(fo[1])), fabsf(fo[2])), 1.0000002f);
+  r.omax = omax;
+  const float reach = __fmul_ru(1.7320509f, __fadd_ru(omax, B));
+  const float D2 = __fmul_ru(D, D);
+  // 2^-29 / 1e-8 and 2^-30 / 1e-8, rounded up
+  const float eps = __fmul_ru(__fmul_ru(0.18626452f, D2), __fadd_ru(reach, D));
+  r.tau = __fmul_ru(__fmul_ru(0.093132258f, D2), __fadd_ru(__fmul_ru(4.f, reach), D));
+  float af[3], lo[3], hi[3], amax = 0.f;
+  int sg[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    const double aa = fabs(a[k]);
-    const double md = 4.76837158203125e-07 * aa * ((double)B + fabs(o[k])) + 1e-30;  // 8 * 2^-24
-    const double pd = md + eps * aa;
-    fo[k] = __double2float_rn(o[k]);
-    if (aa <= 1e30 && md <= 1e30 && pd <= 1e30) {
-      fi[k] = __double2float_rn(a[k]);
-      m[k] = __double2float_ru(md);
-      p[k] = __double2float_ru(pd);
-    } else {  // free axis: this slab never rejects in the filter
-      fi[k] = 0.f;
-      m[k] = __int_as_float(0x7f800000);
-      p[k] = __int_as_float(0x7f800000);
+    const float a = __frcp_rn(fd[k]);  // +-inf for a zero component
+    const float aa = fabsf(a);
+    const float m = __fmul_ru(__fmul_ru(4.7683724e-07f, aa), __fadd_ru(B, __fmul_ru(fabsf(fo[k]), 1.0000002f)));
+    const float c = __fmul_rn(-fo[k], a);
+    sg[k] = fd[k] < 0.f ? 1 : 0;  // a zero component makes the axis free
+    if (aa <= 1e30f && m <= 1e30f && fabsf(c) <= 1e30f) {
+      af[k] = a;
+      lo[k] = __fsub_rd(c, m);
+      hi[k] = __fadd_ru(c, m);
+      amax = fmaxf(amax, aa);
+    } else {  // free axis
+      af[k] = 0.f;
+      lo[k] = __int_as_float(0xff800000);
+      hi[k] = __int_as_float(0x7f800000);
     }
   }
-  r.fox = fo[0], r.foy = fo[1], r.foz = fo[2];
-  r.fix = fi[0], r.fiy = fi[1], r.fiz = fi[2];
-  r.mx = m[0], r.my = m[1], r.mz = m[2];
-  r.px = p[0], r.py = p[1], r.pz = p[2];
+  r.ax = af[0], r.ay = af[1], r.az = af[2];
+  r.lx = lo[0], r.ly = lo[1], r.lz = lo[2];
+  r.hx = hi[0], r.hy = hi[1], r.hz = hi[2];
+  r.sx = sg[0], r.sy = sg[1], r.sz = sg[2];
+  r.dprune = __fmul_ru(eps, __fmul_ru(amax, 1.0000002f));
 }
 
-// Conservative slab filter: true whenever the exact double test
-// (box_exact) is true.  tprune: a lower bound on the entry t of the dilated
-// box, for pruning.
+// The conservative filter: true whenever box_exact is true.  tprune (out):
+// a lower bound on the entry t of the box dilated by eps, for pruning.
 __device__ __forceinline__ bool box_cons(const RayC& r, float lox, float hix, float loy, float hiy, float loz,
                                          float hiz, float& tprune) {
-  const float x1 = __fmul_rn(__fsub_rn(lox, r.fox), r.fix), x2 = __fmul_rn(__fsub_rn(hix, r.fox), r.fix);
-  const float y1 = __fmul_rn(__fsub_rn(loy, r.foy), r.fiy), y2 = __fmul_rn(__fsub_rn(hiy, r.foy), r.fiy);
-  const float z1 = __fmul_rn(__fsub_rn(loz, r.foz), r.fiz), z2 = __fmul_rn(__fsub_rn(hiz, r.foz), r.fiz);
-  const float ax = fminf(x1, x2), bx = fmaxf(x1, x2);
-  const float ay = fminf(y1, y2), by = fmaxf(y1, y2);
-  const float az = fminf(z1, z2), bz = fmaxf(z1, z2);
-  const float L = fmaxf(fmaxf(__fsub_rd(ax, r.mx), __fsub_rd(ay, r.my)), __fsub_rd(az, r.mz));
-  const float U = fminf(fminf(__fadd_ru(bx, r.mx), __fadd_ru(by, r.my)), __fadd_ru(bz, r.mz));
-  tprune = fmaxf(fmaxf(__fsub_rd(ax, r.px), __fsub_rd(ay, r.py)), __fsub_rd(az, r.pz));
+  const float nx = r.sx ? hix : lox, fx = r.sx ? lox : hix;
+  const float ny = r.sy ? hiy : loy, fy = r.sy ? loy : hiy;
+  const float nz = r.sz ? hiz : loz, fz = r.sz ? loz : hiz;
+  const float L = fmaxf(fmaxf(__fmaf_rd(nx, r.ax, r.lx), __fmaf_rd(ny, r.ay, r.ly)), __fmaf_rd(nz, r.az, r.lz));
+  const float U = fminf(fminf(__fmaf_ru(fx, r.ax, r.hx), __fmaf_ru(fy, r.ay, r.hy)), __fmaf_ru(fz, r.az, r.hz));
+  tprune = __fsub_rd(L, r.dprune);
   return L <= U;
 }
 
-// BoundingBox::intersect(const ray&), inc/bbox.h:82-102, in double.
-__device__ __forceinline__ bool box_exact(const RayC& r, float lox, float hix, float loy, float hiy, float loz,
-                                          float hiz) {
+// Certain acceptance: true only when box_exact is certainly true (every
+// exact entry value <= every exact exit value).
+__device__ __forceinline__ bool box_sure(const RayC& r, float lox, float hix, float loy, float hiy, float loz,
+                                         float hiz) {
+  const float nx = r.sx ? hix : lox, fx = r.sx ? lox : hix;
+  const float ny = r.sy ? hiy : loy, fy = r.sy ? loy : hiy;
+  const float nz = r.sz ? hiz : loz, fz = r.sz ? loz : hiz;
+  const float L = fmaxf(fmaxf(__fmaf_ru(nx, r.ax, r.hx), __fmaf_ru(ny, r.ay, r.hy)), __fmaf_ru(nz, r.az, r.hz));
+  const float U = fminf(fminf(__fmaf_rd(fx, r.ax, r.lx), __fmaf_rd(fy, r.ay, r.ly)), __fmaf_rd(fz, r.az, r.lz));
+  return L <= U;
+}
+
+// BoundingBox::intersect(const ray&), inc/bbox.h:82-102, in double.  Kept
+// out of line: it runs only when the filters are not certain.
+static __device__ __noinline__ bool box_exact(double ox, double oy, double oz, double dx, double dy, double dz, float lox,
+                                       float hix, float loy, float hiy, float loz, float hiz) {
+  const double ix = 1.0 / dx, iy = 1.0 / dy, iz = 1.0 / dz;
   double tminx, tmaxx, tminy, tmaxy, tminz, tmaxz;
-  if (r.ix >= 0) {
-    tminx = ((double)lox - r.ox) * r.ix;
-    tmaxx = ((double)hix - r.ox) * r.ix;
+  if (ix >= 0) {
+    tminx = ((double)lox - ox) * ix;
+    tmaxx = ((double)hix - ox) * ix;
   } else {
-    tmaxx = ((double)lox - r.ox) * r.ix;
-    tminx = ((double)hix - r.ox) * r.ix;
+    tmaxx = ((double)lox - ox) * ix;
+    tminx = ((double)hix - ox) * ix;
   }
-  if (r.iy >= 0) {
-    tminy = ((double)loy - r.oy) * r.iy;
-    tmaxy = ((double)hiy - r.oy) * r.iy;
+  if (iy >= 0) {
+    tminy = ((double)loy - oy) * iy;
+    tmaxy = ((double)hiy - oy) * iy;
   } else {
-    tmaxy = ((double)loy - r.oy) * r.iy;
-    tminy = ((double)hiy - r.oy) * r.iy;
+    tmaxy = ((double)loy - oy) * iy;
+    tminy = ((double)hiy - oy) * iy;
   }
-  if (r.iz >= 0) {
-    tminz = ((double)loz - r.oz) * r.iz;
-    tmaxz = ((double)hiz - r.oz) * r.iz;
+  if (iz >= 0) {
+    tminz = ((double)loz - oz) * iz;
+    tmaxz = ((double)hiz - oz) * iz;
   } else {
-    tmaxz = ((double)loz - r.oz) * r.iz;
-    tminz = ((double)hiz - r.oz) * r.iz;
+    tmaxz = ((double)loz - oz) * iz;
+    tminz = ((double)hiz - oz) * iz;
   }
   const double tMin = fmax(fmax(tminx, tminy), tminz);
   const double tMax = fmin(fmin(tmaxx, tmaxy), tmaxz);
   return tMin <= tMax;
 }
 
+// A leaf box: the exact answer, in float when the filters are certain.
+__device__ __forceinline__ bool leaf_box(const RayC& r, float lox, float hix, float loy, float hiy, float loz,
+                                         float hiz) {
+  return box_sure(r, lox, hix, loy, hiy, loz, hiz) ||
+         box_exact(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, lox, hix, loy, hiy, loz, hiz);
+}
+
+// Certain rejection for the triangle test (tri_exact): true only when the
+// double Moller-Trumbore test certainly rejects.  The FP32 determinant and
+// numerators differ from the exact values by at most
+//   E_det = K |AB| |d| |AC|,  E_a = K |d| |AC| (|o| + |T|),
+//   E_b = K |d| |AB| (|o| + |T|)            (max-norms, K = 2^-16),
+// a factor of about 2^2 over a first-order rounding analysis with u = 2^-24
+// (the double computation's own error is far smaller).
+__device__ __forceinline__ bool tri_reject_sure(const RayC& r, float4 a, float4 b, float4 c) {
+  const float ABx = b.x - a.x, ABy = b.y - a.y, ABz = b.z - a.z;
+  const float ACx = c.x - a.x, ACy = c.y - a.y, ACz = c.z - a.z;
+  const float Px = r.fdy * ACz - r.fdz * ACy;
+  const float Py = r.fdz * ACx - r.fdx * ACz;
+  const float Pz = r.fdx * ACy - r.fdy * ACx;
+  const float det = ABx * Px + ABy * Py + ABz * Pz;
+  const float Tx = r.fox - a.x, Ty = r.foy - a.y, Tz = r.foz - a.z;
+  const float an = Tx * Px + Ty * Py + Tz * Pz;
+  const float Qx = Ty * ABz - Tz * ABy;
+  const float Qy = Tz * ABx - Tx * ABz;
+  const float Qz = Tx * ABy - Ty * ABx;
+  const float bn = r.fdx * Qx + r.fdy * Qy + r.fdz * Qz;
+  const float nAB = fmaxf(fmaxf(fabsf(ABx), fabsf(ABy)), fabsf(ABz));
+  const float nAC = fmaxf(fmaxf(fabsf(ACx), fabsf(ACy)), fabsf(ACz));
+  const float nT = fmaxf(fmaxf(fabsf(Tx), fabsf(Ty)), fabsf(Tz));
+  const float nd = fmaxf(fmaxf(fabsf(r.fdx), fabsf(r.fdy)), fabsf(r.fdz));
+  const float K = 1.52587890625e-05f;  // 2^-16
+  const float ot = __fadd_ru(r.omax, nT);
+  const float Ed = __fmul_ru(__fmul_ru(__fmul_ru(K, nAB), nd), nAC);
+  const float Ea = __fmul_ru(__fmul_ru(__fmul_ru(K, nd), nAC), ot);
+  const float Eb = __fmul_ru(__fmul_ru(__fmul_ru(K, nd), nAB), ot);
+  const float ad = fabsf(det);
+  if (__fadd_ru(ad, Ed) < 0.99e-8f) return true;  // |det| < 1e-8 for certain
+  if (!(ad > Ed)) return false;                  // sign of det not certain
+  const float A = det > 0.f ? an : -an, Bv = det > 0.f ? bn : -bn;
+  const float Dhi = __fmul_ru(__fadd_ru(ad, Ed), 1.0000001f);
+  if (__fadd_ru(A, Ea) < 0.f) return true;                  // alpha < 0
+  if (__fsub_rd(A, Ea) > Dhi) return true;                  // alpha > 1
+  if (__fadd_ru(Bv, Eb) < 0.f) return true;                 // beta < 0
+  if (__fsub_rd(__fsub_rd(__fadd_rd(A, Bv), Ea), Eb) > __fadd_ru(Dhi, __fmul_ru(1e-7f, __fadd_ru(fabsf(A), fabsf(Bv)))))
+    return true;                                            // alpha + beta > 1
+  return false;
+}
+
+struct TriHit {
+  double t, alpha, beta;
+  bool hit;
+};
+
 // BVH_d::intersectTriangle, kernels/bvh.cu:297-371: Moller-Trumbore in
 // double without culling; |det| and |t| are compared after rounding to float
-// (fabsf on a double); inclusive edges; negative t accepted.
-__device__ __forceinline__ bool tri_exact(const RayC& r, float4 a, float4 b, float4 c, double& t, double& alpha,
-                                          double& beta) {
+// (fabsf on a double); inclusive edges; negative t accepted.  Out of line:
+// tri_reject_sure settles most tests first.
+static __device__ __noinline__ TriHit tri_exact(double ox, double oy, double oz, double dx, double dy, double dz, float4 a,
+                                         float4 b, float4 c) {
+  TriHit h;
+  h.hit = false;
   const double ax = a.x, ay = a.y, az = a.z;
   const double ABx = (double)b.x - ax, ABy = (double)b.y - ay, ABz = (double)b.z - az;
   const double ACx = (double)c.x - ax, ACy = (double)c.y - ay, ACz = (double)c.z - az;
-  const double Px = r.dy * ACz - r.dz * ACy;
-  const double Py = r.dz * ACx - r.dx * ACz;
-  const double Pz = r.dx * ACy - r.dy * ACx;
+  const double Px = dy * ACz - dz * ACy;
+  const double Py = dz * ACx - dx * ACz;
+  const double Pz = dx * ACy - dy * ACx;
   const double det = ABx * Px + ABy * Py + ABz * Pz;
-  if ((double)fabsf(__double2float_rn(det)) < kRayEps) return false;
+  if ((double)fabsf(__double2float_rn(det)) < kRayEps) return h;
   const double inv = 1 / det;
-  const double Tx = r.ox - ax, Ty = r.oy - ay, Tz = r.oz - az;
+  const double Tx = ox - ax, Ty = oy - ay, Tz = oz - az;
   const double al = (Tx * Px + Ty * Py + Tz * Pz) * inv;
-  if (al < 0 || al > 1) return false;
+  if (al < 0 || al > 1) return h;
   const double Qx = Ty * ABz - Tz * ABy;
   const double Qy = Tz * ABx - Tx * ABz;
   const double Qz = Tx * ABy - Ty * ABx;
-  const double be = (r.dx * Qx + r.dy * Qy + r.dz * Qz) * inv;
-  if (be < 0 || al + be > 1) return false;
+  const double be = (dx * Qx + dy * Qy + dz * Qz) * inv;
+  if (be < 0 || al + be > 1) return h;
   const double tt = (ACx * Qx + ACy * Qy + ACz * Qz) * inv;
-  if ((double)fabsf(__double2float_rn(tt)) < kRayEps) return false;
-  t = tt;
-  alpha = al;
-  beta = be;
-  return true;
+  if ((double)fabsf(__double2float_rn(tt)) < kRayEps) return h;
+  h.t = tt;
+  h.alpha = al;
+  h.beta = be;
+  h.hit = true;
+  return h;
 }
 
 struct HitRec {
@@ -233,13 +319,12 @@ struct HitRec {
   int id;
 };
 
-// The pruning rule: a subtree whose dilated-box entry bound exceeds the
-// best t by more than tau (plus 2^-40 |best| for the rounding of the double
-// slab values themselves) cannot hold a candidate with t <= best, so it can
-// neither win nor tie; skipping it leaves the closest hit and its left-first
-// tie-break unchanged.
-__device__ __forceinline__ bool prune_ok(float tprune, float tau, double best) {
-  return (double)tprune > best + (double)tau + 9.094947017729282e-13 * fabs(best);
+// The pruning bound for the current best t, rounded up to float: best +
+// tau + 2^-40 |best|.  A subtree with tprune > this bound cannot hold a
+// candidate with t <= best, so it can neither win nor tie; skipping it leaves
+// the closest hit and its left-first tie-break unchanged.
+__device__ __forceinline__ float prune_bound(double best, float tau) {
+  return __double2float_ru(best + (double)tau + 9.094947017729282e-13 * fabs(best));
 }
 
 // BVH_d::intersect (ANY = false: closest hit, ties to the first hit in
@@ -262,8 +347,9 @@ __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, float rb
   float tp;
   if (!box_cons(r, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], tp)) return 0;
   int node = S.root;
-  if (node < 0 && !box_exact(r, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5])) return 0;
+  if (node < 0 && !leaf_box(r, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5])) return 0;
   bool have = false;
+  float pb = __int_as_float(0x7f800000);  // prune bound; +inf until a hit
   int2 stack[kStackSize];
   int sp = 0;
   // a valid tree visits each node at most once per ray; the bound and the
@@ -279,11 +365,11 @@ __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, float rb
       float tl, tr;
       bool hl = box_cons(r, xl.x, xl.y, xl.z, xl.w, zz.x, zz.y, tl);
       bool hr = box_cons(r, xr.x, xr.y, xr.z, xr.w, zz.z, zz.w, tr);
-      if (hl && ch.x < 0) hl = box_exact(r, xl.x, xl.y, xl.z, xl.w, zz.x, zz.y);
-      if (hr && ch.y < 0) hr = box_exact(r, xr.x, xr.y, xr.z, xr.w, zz.z, zz.w);
-      if (!ANY && have) {
-        if (hl && prune_ok(tl, r.tau, h.t)) hl = false;
-        if (hr && prune_ok(tr, r.tau, h.t)) hr = false;
+      if (hl && ch.x < 0) hl = leaf_box(r, xl.x, xl.y, xl.z, xl.w, zz.x, zz.y);
+      if (hr && ch.y < 0) hr = leaf_box(r, xr.x, xr.y, xr.z, xr.w, zz.z, zz.w);
+      if (!ANY) {
+        hl = hl && !(tl > pb);
+        hr = hr && !(tr > pb);
       }
       if (hl) {
         if (hr) {
@@ -301,8 +387,11 @@ __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, float rb
       if (STATS) ts->tris++;
       const float4* lp = reinterpret_cast<const float4*>(S.leaves + (~node));
       const float4 a = __ldg(lp), b = __ldg(lp + 1), c = __ldg(lp + 2);
-      double t, al, be;
-      if (tri_exact(r, a, b, c, t, al, be)) {
+      TriHit th;
+      th.hit = false;
+      if (!tri_reject_sure(r, a, b, c)) th = tri_exact(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, a, b, c);
+      if (th.hit) {
+        const double t = th.t, al = th.alpha, be = th.beta;
         if (ANY) {
           h.t = t, h.alpha = al, h.beta = be, h.id = __float_as_int(a.w);
           return 1;
@@ -310,6 +399,7 @@ __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, float rb
         if (!have || t < h.t) {
           h.t = t, h.alpha = al, h.beta = be, h.id = __float_as_int(a.w);
           have = true;
+          pb = prune_bound(t, r.tau);
         }
       }
     }
@@ -317,7 +407,7 @@ __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, float rb
     bool next = false;
     while (sp > 0) {
       const int2 e = stack[--sp];
-      if (!ANY && have && prune_ok(__int_as_float(e.y), r.tau, h.t)) continue;
+      if (!ANY && __int_as_float(e.y) > pb) continue;
       node = e.x;
       next = true;
       break;

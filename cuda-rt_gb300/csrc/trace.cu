@@ -45,7 +45,7 @@ __device__ __forceinline__ DMat load_mat(const DScene& S, int tri) {
 constexpr int kTileW = 8, kTileH = 4;
 
 template <bool STATS>
-__global__ void __launch_bounds__(128) k_render(DScene S, RenderArgs A) {
+__global__ void __launch_bounds__(128, 4) k_render(DScene S, RenderArgs A) {
   TravStats ts;
   float rb[6], B, D;
   scene_consts(S, rb, B, D);
