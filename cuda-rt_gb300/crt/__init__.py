@@ -20,7 +20,7 @@ import numpy as np
 from . import data  # noqa: F401
 from .build import LIB as LIB_PATH
 
-__all__ = ["CrtError", "Scene", "lib", "sort_pairs", "morton", "STATUS", "render_args"]
+__all__ = ["CrtError", "Scene", "lib", "sort_pairs", "sort_pairs_noalloc", "morton", "STATUS", "render_args"]
 
 STATUS = {0: "CRT_OK", 1: "CRT_INVALID_ARG", 2: "CRT_OOM", 3: "CRT_CUDA_ERROR", 4: "CRT_STACK_OVERFLOW",
           5: "CRT_TIMEOUT", 6: "CRT_NOT_BUILT"}
@@ -86,6 +86,7 @@ def lib():
             "crt_render": [vp, vp, vp, vp, vp, vp],
             "crt_morton": [vp, vp, i32, vp, vp, vp],
             "crt_sort_pairs": [vp, vp, vp, vp, i32, i32, vp],
+            "crt_sort_pairs_noalloc": [vp, vp, vp, vp, i32, i32, vp],
             "crt_scene_check": [vp, vp],
         }
         for name, args in sig.items():
@@ -241,6 +242,16 @@ def sort_pairs(keys_in, vals_in, keys_out, vals_out, key_bits=32, stream=None):
     """crt_sort_pairs on device tensors (stable LSD radix sort)."""
     _check(lib().crt_sort_pairs(_addr(keys_in), _addr(vals_in), _addr(keys_out), _addr(vals_out),
                                 int(keys_in.shape[0]), key_bits, _stream(stream)))
+
+
+def sort_pairs_noalloc(keys_in, vals_in, keys_out, vals_out, key_bits=32, stream=None):
+    """crt_sort_pairs_noalloc on device tensors: the same sort with its scratch
+    in a fixed device array (at most CRT_SORT_NOALLOC_MAX_PAIRS pairs)."""
+    _check(lib().crt_sort_pairs_noalloc(_addr(keys_in), _addr(vals_in), _addr(keys_out), _addr(vals_out),
+                                        int(keys_in.shape[0]), key_bits, _stream(stream)))
+
+
+SORT_NOALLOC_MAX_PAIRS = 1 << 20
 
 
 def camera_angle(fov):

@@ -129,6 +129,11 @@ void free_scene(crt_scene* s) {
 
 }  // namespace
 
+namespace crt {
+// Lets entry points in other translation units record their error message.
+void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace crt
+
 extern "C" {
 
 const char* crt_last_error_string(void) { return g_err.c_str(); }

@@ -165,6 +165,24 @@ crt_status crt_morton(const float* vertices, const int32_t* vertex_indices, int3
 crt_status crt_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
                           int32_t n, int32_t key_bits, void* stream);
 
+/* No counterpart in the reference.  The same stable radix sort as
+ * crt_sort_pairs, for callers that must not allocate device memory where they
+ * sort: cudaMalloc synchronises the whole device (a per-frame rebuild would
+ * stall on it every frame), some host frameworks forbid a plugin from
+ * allocating on its own, and a hot-path sort must not fail with
+ * out-of-memory mid-frame.  Its scratch is a fixed device array of about
+ * 16.8 MB inside libcrt.so, held on every GPU that loads the library until
+ * the process exits; n may not exceed CRT_SORT_NOALLOC_MAX_PAIRS (larger n:
+ * CRT_INVALID_ARG, nothing launched).  No cudaMalloc/cudaFree or other
+ * allocating call is made.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) with that device current; make that
+ * first call before any stream capture.  All calls share the array: each
+ * clears what must start at zero, and calls whose work overlaps on the GPU
+ * race.  Device pointers only; synchronises `stream`. */
+#define CRT_SORT_NOALLOC_MAX_PAIRS (1 << 20)
+crt_status crt_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                                  uint32_t* vals_out, int32_t n, int32_t key_bits, void* stream);
+
 /* Synchronise `stream` and report device-side errors the scene's kernels
  * recorded (stack overflow, bounded-wait timeout, non-finite input). */
 crt_status crt_scene_check(crt_scene* scene, void* stream);
