@@ -84,16 +84,31 @@ __global__ void __launch_bounds__(256) k_bounds(const float* __restrict__ V, con
     }
     e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, off));
   }
-  const bool all_ok = __all_sync(0xffffffffu, ok);
-  if ((threadIdx.x & 31) == 0) {
+  // block reduction, then one set of atomics per block
+  __shared__ float s_red[8][7];
+  __shared__ int s_bad;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_bad = 0;
+  __syncthreads();
+  if (!__all_sync(0xffffffffu, ok) && lane == 0) s_bad = 1;
+  if (lane == 0) {
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-      atomicMin(&g->bmin[k], f2ord(lo[k]));
-      atomicMax(&g->bmax[k], f2ord(hi[k]));
-    }
-    atomicMax(&g->emax, f2ord(e));
-    if (!all_ok) atomicOr(&g->err, kErrNonFinite);
+    for (int k = 0; k < 3; k++) s_red[warp][k] = lo[k], s_red[warp][3 + k] = hi[k];
+    s_red[warp][6] = e;
   }
+  __syncthreads();
+  if (threadIdx.x < 7) {
+    const int k = threadIdx.x;
+    float v = s_red[0][k];
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) v = (k < 3) ? fminf(v, s_red[w][k]) : fmaxf(v, s_red[w][k]);
+    if (k < 3)
+      atomicMin(&g->bmin[k], f2ord(v));
+    else if (k < 6)
+      atomicMax(&g->bmax[k - 3], f2ord(v));
+    else
+      atomicMax(&g->emax, f2ord(v));
+  }
+  if (threadIdx.x == 0 && s_bad) atomicOr(&g->err, kErrNonFinite);
 }
 
 __device__ __forceinline__ uint32_t expand_bits(uint32_t v) {  // ExpandBits, kernels/bvh.cu:13-21
@@ -114,24 +129,74 @@ __device__ __forceinline__ uint32_t morton_axis(double p) {
   return (uint32_t)__double2float_rn(s);
 }
 
-// computeMortonCodesKernel, kernels/bvh.cu:37-61, in double as the reference.
-__device__ __forceinline__ uint32_t morton_code(const float lo[3], const float hi[3], const double mn[3],
-                                                const double mx[3]) {
-  uint32_t e[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    double c = 0.5 * ((double)lo[k] + (double)hi[k]);
-    c = (c - mn[k]) / (mx[k] - mn[k]);
-    e[k] = expand_bits(morton_axis(c));
-  }
-  return e[0] * 4 + e[1] * 2 + e[2];
+// computeMortonCodesKernel, kernels/bvh.cu:37-61, in double as the reference:
+// c = 0.5*(lo+hi), q = (c-mn)/(mx-mn), cell = trunc(RN32(clamp(1024 q))).
+static __device__ __noinline__ uint32_t morton_axis_exact(float lo, float hi, double mn, double mx) {
+  double c = 0.5 * ((double)lo + (double)hi);
+  c = (c - mn) / (mx - mn);
+  return morton_axis(c);
 }
 
-__device__ __forceinline__ void load_scene_box(const SceneGlobals* g, double mn[3], double mx[3]) {
+// Exact sum a + b as an unevaluated pair (s, e): s = RN(a + b), e the error.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// The same cell without double arithmetic whenever that is provably right.
+// y = 1024 (c - mn) / (mx - mn) is formed in float-float: c = (lo + hi)/2,
+// c - mn and mx - mn by exact two-sums, then one division with an FMA-based
+// correction, so y_hi + y_lo is within E = 2^-30 (|y| + 1024 (|c| + |mn|)/den)
+// of the exact quotient (about 2^10 over a first-order bound; the double path's
+// own error is smaller still).  The cell is floor(y) unless y sits within half
+// a float ulp (<= 2^-15 below 1024) of the next integer, or the bound does not
+// separate y from an integer: then the double path decides.
+__device__ __forceinline__ uint32_t morton_cell(float lo, float hi, float mn, float mx) {
+  float dh, dl;
+  two_sum(mx, -mn, dh, dl);
+  if (dh > 0.f) {
+    float sh, sl;
+    two_sum(lo, hi, sh, sl);
+    const float ch = 0.5f * sh, cl = 0.5f * sl;  // exact halving
+    float nh, nl;
+    two_sum(ch, -mn, nh, nl);
+    nl = __fadd_rn(nl, cl);
+    const float q1 = __fdiv_rn(nh, dh);
+    // r = (nh + nl) - q1 (dh + dl), with q1*dh split exactly by an FMA
+    const float ph = __fmul_rn(q1, dh);
+    const float pl = __fmaf_rn(q1, dh, -ph);
+    const float r = __fadd_rn(__fsub_rn(__fsub_rn(nh, ph), pl), __fsub_rn(nl, __fmul_rn(q1, dl)));
+    const float q2 = __fdiv_rn(r, dh);
+    const float yh = 1024.f * q1, yl = 1024.f * q2;  // exact scaling
+    const float E = __fmul_ru(9.3132257e-10f, __fadd_ru(fabsf(yh), __fmul_ru(1024.f, __fdiv_ru(__fadd_ru(fabsf(ch),
+                                                                                                   fabsf(mn)), dh))));
+    if (__fadd_ru(__fadd_ru(yh, yl), E) < 0.f) return 0u;
+    if (__fsub_rd(__fsub_rd(yh, -yl), E) > 1023.f) return 1023u;
+    const float fl = floorf(yh);
+    if (fl >= 0.f && fl <= 1023.f) {
+      const float fr = __fsub_rn(yh, fl);  // exact: fl <= yh < fl + 1
+      // need fr + yl in [E, 1 - 2^-14 - E)
+      if (__fsub_rd(__fadd_rd(fr, yl), E) >= 0.f && __fadd_ru(__fadd_ru(fr, yl), E) < 0.99993896484375f)
+        return (uint32_t)fl;
+    }
+  }
+  return morton_axis_exact(lo, hi, (double)mn, (double)mx);
+}
+
+__device__ __forceinline__ uint32_t morton_code(const float lo[3], const float hi[3], const float mn[3],
+                                                const float mx[3]) {
+  const uint32_t ex = expand_bits(morton_cell(lo[0], hi[0], mn[0], mx[0]));
+  const uint32_t ey = expand_bits(morton_cell(lo[1], hi[1], mn[1], mx[1]));
+  const uint32_t ez = expand_bits(morton_cell(lo[2], hi[2], mn[2], mx[2]));
+  return ex * 4 + ey * 2 + ez;
+}
+
+__device__ __forceinline__ void load_scene_box(const SceneGlobals* g, float mn[3], float mx[3]) {
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    mn[k] = (double)ord2f(g->bmin[k]);
-    mx[k] = (double)ord2f(g->bmax[k]);
+    mn[k] = ord2f(g->bmin[k]);
+    mx[k] = ord2f(g->bmax[k]);
   }
 }
 
@@ -143,16 +208,29 @@ __global__ void __launch_bounds__(512) k_morton(const float* __restrict__ V, con
   __shared__ uint32_t sh[3 * kRadix];
   for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) sh[i] = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < status_words; i += gridDim.x * blockDim.x) status[i] = 0;
-  double mn[3], mx[3];
+  float mn[3], mx[3];
   load_scene_box(g, mn, mx);
   __syncthreads();
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-    float3 a, b, c;
-    float lo[3], hi[3];
-    tri_box(V, vidx, t, a, b, c, lo, hi);
-    const uint32_t code = morton_code(lo, hi, mn, mx);
-    keys[t] = code;
-    for (int p = 0; p < passes; p++) atomicAdd(&sh[p * kRadix + ((code >> (p * kRadixBits)) & (kRadix - 1))], 1u);
+  // four triangles per thread per round: their loads overlap
+  const int stride = gridDim.x * blockDim.x;
+  for (int t0 = blockIdx.x * blockDim.x + threadIdx.x; t0 < n; t0 += 4 * stride) {
+    float lo[4][3], hi[4][3];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int t = t0 + u * stride;
+      float3 a, b, c;
+      if (t < n) tri_box(V, vidx, t, a, b, c, lo[u], hi[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int t = t0 + u * stride;
+      if (t < n) {
+        const uint32_t code = morton_code(lo[u], hi[u], mn, mx);
+        keys[t] = code;
+        for (int p = 0; p < passes; p++)
+          atomicAdd(&sh[p * kRadix + ((code >> (p * kRadixBits)) & (kRadix - 1))], 1u);
+      }
+    }
   }
   __syncthreads();
   for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x)
@@ -162,7 +240,7 @@ __global__ void __launch_bounds__(512) k_morton(const float* __restrict__ V, con
 // Standalone Morton codes against a given scene box (crt_morton).
 __global__ void k_morton_only(const float* __restrict__ V, const int* __restrict__ vidx, int n,
                               const float* __restrict__ box6, uint32_t* __restrict__ keys) {
-  double mn[3], mx[3];
+  float mn[3], mx[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) mn[k] = box6[k], mx[k] = box6[3 + k];
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
@@ -191,6 +269,12 @@ __global__ void __launch_bounds__(512) k_key_hist(const uint32_t* __restrict__ k
 
 __global__ void k_zero_u32(uint32_t* p, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = 0;
+}
+
+__device__ __forceinline__ int atomic_add_acq_rel(int* p, int v) {
+  int old;
+  asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
 }
 
 __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
@@ -306,29 +390,44 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
   for (int j = 0; j < 4; j++) st_relaxed(my + 4 * tid + j, (tile == 0 ? kFlagInc : kFlagAgg) | cnt[j]);
   uint32_t pre[4] = {0, 0, 0, 0};
   if (tile > 0) {
-#pragma unroll 1
-    for (int j = 0; j < 4; j++) {
-      const int d = 4 * tid + j;
-      uint32_t acc = 0;
-      for (int look = tile - 1; look >= 0; look--) {
-        const uint32_t* p = status + (size_t)look * kRadix + d;
-        uint32_t s = ld_relaxed(p);
-        int spins = 0;
-        while ((s & ~kValMask) == 0) {
-          // bounded wait; once any wait has timed out, later ones give up at once
-          if (++spins > kSpinLimit || ((spins & 1023) == 0 && (ld_relaxed((const uint32_t*)err) & kErrTimeout))) {
-            atomicOr(err, kErrTimeout);
-            s = kFlagInc;
-            break;
-          }
-          __nanosleep(64);
-          s = ld_relaxed(p);
+    // The thread's four digits walk back together: four independent loads
+    // per L2 round trip.  A walk stops at the first inclusive prefix.
+    int look[4] = {tile - 1, tile - 1, tile - 1, tile - 1};
+    int spins = 0;
+    uint32_t live = 0xF;
+    while (live) {
+      uint32_t sv[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        sv[j] = (live >> j) & 1 ? ld_relaxed(status + (size_t)look[j] * kRadix + 4 * tid + j) : 0u;
+      bool waiting = false;
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        if (!((live >> j) & 1)) continue;
+        const uint32_t f = sv[j] & ~kValMask;
+        if (f == 0) {
+          waiting = true;
+          continue;
         }
-        acc += s & kValMask;
-        if ((s & ~kValMask) == kFlagInc) break;
+        pre[j] += sv[j] & kValMask;
+        if (f == kFlagInc || look[j] == 0) {
+          live &= ~(1u << j);
+          st_relaxed(my + 4 * tid + j, kFlagInc | (pre[j] + cnt[j]));
+        } else {
+          look[j]--;
+        }
       }
-      pre[j] = acc;
-      st_relaxed(my + d, kFlagInc | (acc + cnt[j]));
+      if (waiting) {
+        // bounded wait; once any wait has timed out, later ones give up at once
+        if (++spins > kSpinLimit || ((spins & 1023) == 0 && (ld_relaxed((const uint32_t*)err) & kErrTimeout))) {
+          atomicOr(err, kErrTimeout);
+#pragma unroll
+          for (int j = 0; j < 4; j++)
+            if ((live >> j) & 1) st_relaxed(my + 4 * tid + j, kFlagInc | (pre[j] + cnt[j]));
+          break;
+        }
+        __nanosleep(32);
+      }
     }
   }
   uint32_t ctot;
@@ -365,60 +464,97 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
   }
 }
 
-// delta(), kernels/bvh.cu:71-88 (i is always in range here).
-__device__ __forceinline__ int kdelta(const uint32_t* __restrict__ c, int n, int i, int j) {
+// delta(), kernels/bvh.cu:71-88: with the augmented key (code << 32 | index)
+// the common-prefix length is one 64-bit clz -- clz(ci ^ cj) when the codes
+// differ, 32 + clz(i ^ j) when they are equal, exactly the reference's two
+// cases; -1 out of range.
+__device__ __forceinline__ int kdelta(const uint32_t* __restrict__ c, int n, uint64_t ki, int j) {
   if (j < 0 || j >= n) return -1;
-  const uint32_t a = __ldg(c + i), b = __ldg(c + j);
-  return a != b ? __clz((int)(a ^ b)) : 32 + __clz(i ^ j);
+  const uint64_t kj = ((uint64_t)__ldg(c + j) << 32) | (uint32_t)j;
+  return __clzll((long long)(ki ^ kj));
 }
+
+// The parent word of a node: parent index | bit 31 when the node is its
+// parent's left child | bit 30 when the parent's leaf range crosses a
+// kRefitBlock boundary (the refit then meets at gpu scope).
+constexpr int kRefitBlock = 512;
+constexpr uint32_t kParentLeft = 1u << 31, kParentSpans = 1u << 30, kParentMask = (1u << 30) - 1;
 
 // BuildHierarchy (kernels/bvh.cu:164-207) with FindSpan (bvh.cu:100-133) and
 // FindSplit (bvh.cu:134-162): one thread per internal node writes its child
-// codes, the children's parents, and clears the node's refit flag.
+// codes, its children's parent words, and clears the node's refit flag.
 __global__ void __launch_bounds__(256) k_hierarchy(const uint32_t* __restrict__ codes, int n, BNode* __restrict__ nodes,
-                                                   int* __restrict__ parent, int* __restrict__ flags) {
+                                                   uint32_t* __restrict__ parent, int* __restrict__ flags) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n - 1) return;
-  const int dd = kdelta(codes, n, i, i + 1) - kdelta(codes, n, i, i - 1);
+  const uint64_t ki = ((uint64_t)__ldg(codes + i) << 32) | (uint32_t)i;
+  const int dd = kdelta(codes, n, ki, i + 1) - kdelta(codes, n, ki, i - 1);
   const int d = dd > 0 ? 1 : (dd < 0 ? -1 : 0);
-  const int dmin = kdelta(codes, n, i, i - d);
+  const int dmin = kdelta(codes, n, ki, i - d);
   int lmax = 2;
-  while (kdelta(codes, n, i, i + lmax * d) > dmin) lmax *= 2;
+  while (kdelta(codes, n, ki, i + lmax * d) > dmin) lmax *= 2;
   int l = 0, t = lmax;
   do {
     t /= 2;
-    if (kdelta(codes, n, i, i + (l + t) * d) > dmin) l += t;
+    if (kdelta(codes, n, ki, i + (l + t) * d) > dmin) l += t;
   } while (t > 1);
   const int lo = min(i, i + l * d), hi = max(i, i + l * d);
   int left = lo, right = hi;
-  const int same = kdelta(codes, n, left, right);
+  uint64_t kl = ((uint64_t)__ldg(codes + left) << 32) | (uint32_t)left;
+  const int same = kdelta(codes, n, kl, right);
   do {
     const int s = (right + left) / 2;
-    if (kdelta(codes, n, left, s) > same)
+    if (kdelta(codes, n, kl, s) > same) {
       left = s;
-    else
+      kl = ((uint64_t)__ldg(codes + left) << 32) | (uint32_t)left;
+    } else {
       right = s;
+    }
   } while (right > left + 1);
   const int split = left;
   const int c1 = (split == lo) ? ~split : split;
   const int c2 = (split + 1 == hi) ? ~(split + 1) : split + 1;
   nodes[i].child = make_int4(c1, c2, 0, 0);
-  parent[c1 < 0 ? (n - 1) + split : split] = i;
-  parent[c2 < 0 ? (n - 1) + split + 1 : split + 1] = i;
+  const uint32_t spans = (lo / kRefitBlock != hi / kRefitBlock) ? kParentSpans : 0u;
+  parent[c1 < 0 ? (n - 1) + split : split] = (uint32_t)i | kParentLeft | spans;
+  parent[c2 < 0 ? (n - 1) + split + 1 : split + 1] = (uint32_t)i | spans;
   flags[i] = 0;
 }
 
 // RefitBounds (kernels/bvh.cu:209-258): one climber per leaf; at each node the
 // first arrival stops and the second computes the union (bboxunion,
-// bvh.cu:63-69) and climbs on.  Boxes are stored in the parent's child slot.
-// Flags count arrivals; each refit adds exactly two per node, so the parity
-// of the old value tells first from second without clearing between refits.
-// Also writes the sorted leaf triangles and the largest triangle extent.
-__global__ void __launch_bounds__(256) k_refit(const float* __restrict__ V, const int* __restrict__ vidx,
-                                               const uint32_t* __restrict__ ids, int n, BNode* nodes,
-                                               LeafTri* __restrict__ leaves, const int* __restrict__ parent,
-                                               int* flags, SceneGlobals* g) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+// bvh.cu:63-69) and climbs on.  min/max are exact, so every schedule gives the
+// reference's boxes.  Boxes are stored in the parent's child slot (BNode).
+//
+// A block owns kRefitBlock consecutive sorted leaves.  A node whose leaf
+// range lies inside that span has both children's climbers in the block, so
+// its two arrivals meet in shared memory with block-scope ordering (most
+// nodes).  A node spanning several blocks uses the global flag with
+// release/acquire at gpu scope.  Global flags count arrivals; each refit adds
+// exactly two per spanning node, so the parity of the old value tells first
+// from second without clearing between refits.  Each climb step needs one
+// dependent load: the parent word (index, side, spanning bit).
+__device__ __forceinline__ void put_slot(BNode* P, bool left, const float lo[3], const float hi[3]) {
+  if (left) {
+    __stcg(&P->xy_l, make_float4(lo[0], hi[0], lo[1], hi[1]));
+    __stcg(reinterpret_cast<float2*>(&P->z_lr), make_float2(lo[2], hi[2]));
+  } else {
+    __stcg(&P->xy_r, make_float4(lo[0], hi[0], lo[1], hi[1]));
+    __stcg(reinterpret_cast<float2*>(&P->z_lr) + 1, make_float2(lo[2], hi[2]));
+  }
+}
+
+__global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__ V, const int* __restrict__ vidx,
+                                                       const uint32_t* __restrict__ ids, int n, BNode* nodes,
+                                                       LeafTri* __restrict__ leaves,
+                                                       const uint32_t* __restrict__ parent, int* flags,
+                                                       SceneGlobals* g) {
+  __shared__ float s_box[kRefitBlock][2][6];  // children's boxes at each block-local node
+  __shared__ int s_flag[kRefitBlock];
+  s_flag[threadIdx.x] = 0;
+  __syncthreads();
+  const int k0 = blockIdx.x * kRefitBlock;
+  const int k = k0 + threadIdx.x;
   float e = 0.f;
   bool ok = true;
   if (k < n) {
@@ -437,39 +573,42 @@ __global__ void __launch_bounds__(256) k_refit(const float* __restrict__ V, cons
 #pragma unroll
       for (int q = 0; q < 3; q++) g->root_box[q] = lo[q], g->root_box[3 + q] = hi[q];
     } else {
-      int code = ~k;
-      int p = __ldg(parent + (n - 1) + k);
-      // a valid tree is at most 59 levels deep (CRT_MAX_TRIANGLES); the
-      // bound only guards against a corrupt parent chain
+      uint32_t w = __ldg(parent + (n - 1) + k);
       for (int level = 0;; level++) {
-        if (level >= kStackSize || p < 0 || p >= n - 1) {
+        const int p = (int)(w & kParentMask);
+        if (level >= kStackSize || p >= n - 1) {  // only a corrupt tree gets here
           atomicOr(&g->err, kErrStack);
           break;
         }
+        const uint32_t wn = (p == 0) ? 0u : __ldg(parent + p);  // next step's word, issued early
         BNode* P = nodes + p;
-        const bool is_left = (__ldcg(&P->child.x) == code);
-        if (is_left) {
-          __stcg(&P->xy_l, make_float4(lo[0], hi[0], lo[1], hi[1]));
-          __stcg(reinterpret_cast<float2*>(&P->z_lr), make_float2(lo[2], hi[2]));
+        const bool is_left = (w & kParentLeft) != 0;
+        put_slot(P, is_left, lo, hi);
+        if (!(w & kParentSpans)) {  // both arrivals are threads of this block
+          const int sl = p - k0;
+          float* mine = s_box[sl][is_left ? 0 : 1];
+#pragma unroll
+          for (int q = 0; q < 3; q++) mine[q] = lo[q], mine[3 + q] = hi[q];
+          __threadfence_block();
+          if (atomicAdd(&s_flag[sl], 1) == 0) break;  // first arrival
+          __threadfence_block();
+          const volatile float* o = s_box[sl][is_left ? 1 : 0];
+#pragma unroll
+          for (int q = 0; q < 3; q++) lo[q] = fminf(lo[q], o[q]), hi[q] = fmaxf(hi[q], o[3 + q]);
         } else {
-          __stcg(&P->xy_r, make_float4(lo[0], hi[0], lo[1], hi[1]));
-          __stcg(reinterpret_cast<float2*>(&P->z_lr) + 1, make_float2(lo[2], hi[2]));
+          // spanning node: release our slot, acquire the sibling's (gpu scope)
+          if ((atomic_add_acq_rel(flags + p, 1) & 1) == 0) break;  // first arrival
+          const float4 xl = __ldcg(&P->xy_l), xr = __ldcg(&P->xy_r), zz = __ldcg(&P->z_lr);
+          lo[0] = fminf(xl.x, xr.x), hi[0] = fmaxf(xl.y, xr.y);
+          lo[1] = fminf(xl.z, xr.z), hi[1] = fmaxf(xl.w, xr.w);
+          lo[2] = fminf(zz.x, zz.z), hi[2] = fmaxf(zz.y, zz.w);
         }
-        __threadfence();
-        const int old = atomicAdd(flags + p, 1);
-        if ((old & 1) == 0) break;  // first arrival: the sibling finishes this node
-        __threadfence();
-        const float4 xl = __ldcg(&P->xy_l), xr = __ldcg(&P->xy_r), zz = __ldcg(&P->z_lr);
-        lo[0] = fminf(xl.x, xr.x), hi[0] = fmaxf(xl.y, xr.y);
-        lo[1] = fminf(xl.z, xr.z), hi[1] = fmaxf(xl.w, xr.w);
-        lo[2] = fminf(zz.x, zz.z), hi[2] = fmaxf(zz.y, zz.w);
         if (p == 0) {
 #pragma unroll
           for (int q = 0; q < 3; q++) g->root_box[q] = lo[q], g->root_box[3 + q] = hi[q];
           break;
         }
-        code = p;
-        p = __ldg(parent + p);
+        w = wn;
       }
     }
   }
@@ -482,6 +621,18 @@ __global__ void __launch_bounds__(256) k_refit(const float* __restrict__ V, cons
   }
 }
 
+}  // namespace
+
+namespace {
+__global__ void k_refit_init(SceneGlobals* g) {
+  if (threadIdx.x == 0) g->emax = f2ord(0.f);
+}
+
+void refit(const MeshBufs& m, const BuildBufs& b, cudaStream_t st) {
+  const int n = m.ntri;
+  k_refit<<<(n + kRefitBlock - 1) / kRefitBlock, kRefitBlock, 0, st>>>(m.verts, m.vidx, b.vals_b, n, b.nodes,
+                                                                        b.leaves, b.parent, b.flags, b.g);
+}
 }  // namespace
 
 int num_sms() {
@@ -519,15 +670,15 @@ cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st)
     vin = vo;
   }
   if (n >= 2) k_hierarchy<<<(n - 1 + 255) / 256, 256, 0, st>>>(b.keys_b, n, b.nodes, b.parent, b.flags);
-  k_refit<<<(n + 255) / 256, 256, 0, st>>>(m.verts, m.vidx, b.vals_b, n, b.nodes, b.leaves, b.parent, b.flags, b.g);
+  refit(m, b, st);
   return cudaGetLastError();
 }
 
 cudaError_t launch_refit(const MeshBufs& m, const BuildBufs& b, cudaStream_t st) {
   const int n = m.ntri;
   if (n <= 0) return cudaSuccess;
-  cudaMemsetAsync(&b.g->emax, 0, sizeof(int), st);  // f2ord(0.f) == 0
-  k_refit<<<(n + 255) / 256, 256, 0, st>>>(m.verts, m.vidx, b.vals_b, n, b.nodes, b.leaves, b.parent, b.flags, b.g);
+  k_refit_init<<<1, 32, 0, st>>>(b.g);
+  refit(m, b, st);
   return cudaGetLastError();
 }
 

@@ -209,7 +209,7 @@ crt_status crt_scene_create(const crt_mesh_desc* d, void* stream, crt_scene** ou
   b.vals_b = reinterpret_cast<uint32_t*>(base + off[3]);
   b.hist = reinterpret_cast<uint32_t*>(base + off[4]);
   b.status = reinterpret_cast<uint32_t*>(base + off[5]);
-  b.parent = reinterpret_cast<int*>(base + off[6]);
+  b.parent = reinterpret_cast<uint32_t*>(base + off[6]);
   b.flags = reinterpret_cast<int*>(base + off[7]);
   b.nodes = reinterpret_cast<BNode*>(base + off[8]);
   b.leaves = reinterpret_cast<LeafTri*>(base + off[9]);
@@ -317,7 +317,7 @@ crt_status crt_bvh_export(crt_scene* s, float* scene_box, int32_t* codes, uint32
   std::vector<int> n3(3 * nn);
   std::vector<float> nb(6 * nn);
   auto ref = [n](int code) { return code >= 0 ? code : (n - 1) + ~code; };
-  for (size_t i = 0; i < nn; i++) n3[3 * i] = (i == 0) ? -1 : parent[i];
+  for (size_t i = 0; i < nn; i++) n3[3 * i] = (i == 0) ? -1 : (int)((uint32_t)parent[i] & ((1u << 30) - 1));
   for (int k = 0; k < n; k++) {
     n3[3 * ((n - 1) + k) + 1] = (int)hv[k];
     n3[3 * ((n - 1) + k) + 2] = (int)hv[k];

@@ -24,7 +24,7 @@ struct BuildBufs {
   uint32_t *keys_a = nullptr, *keys_b = nullptr, *vals_a = nullptr, *vals_b = nullptr;
   uint32_t* hist = nullptr;    // 3 * kRadix
   uint32_t* status = nullptr;  // 3 * tiles * kRadix
-  int* parent = nullptr;       // 2n - 1, reference numbering
+  uint32_t* parent = nullptr;  // 2n - 1: parent index (reference numbering) | left-child and spanning bits
   int* flags = nullptr;        // n - 1
   BNode* nodes = nullptr;      // n - 1
   LeafTri* leaves = nullptr;   // n
