@@ -91,7 +91,7 @@ class Clocks:
         sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
         mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if "Active" in s[3 + i]})
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].strip() == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.samples)}
 
@@ -205,6 +205,7 @@ def run_crt(args, dist, rank, ws):
     e2e_value = rays * e2e_steps * ws / t_e2e / 1e6
     ok_img = bool(np.array_equal(rgb_h.numpy(), rgb.cpu().numpy()))
 
+    refit = run_refit_vs_rebuild() if (rank == 0 and not args.no_extras) else None
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(sc, args.cpu_seconds)
@@ -232,9 +233,53 @@ def run_crt(args, dist, rank, ws):
         "gpu_launches": 9 * args.steps,
         "clocks": clk.summary(),
     }
+    if refit is not None:
+        line["refit_vs_rebuild"] = refit
     if cpu is not None:
         line["cpu_baseline"] = cpu
     return line
+
+
+def run_refit_vs_rebuild(frames=60, W2=1280, H2=720, spp=4):
+    """The dynamic workload: the large mesh animated over `frames` frames, each
+    frame traced at W2 x H2 x spp; per frame either an atomic bottom-up refit on
+    frame 0's topology or a full LBVH rebuild.  Vertex arrays of all frames are
+    resident on the device before timing; each frame's update (vertex copy +
+    refit or rebuild) and render are timed with CUDA events."""
+    import torch
+
+    import crt
+    from crt import data
+    anim = data.Animation(frames=frames)
+    sc = anim.scene(W2, H2, spp)
+    allv = torch.from_numpy(np.stack([anim.vertices(f) for f in range(frames)])).cuda()
+    stream = torch.cuda.current_stream()
+    rgb = torch.empty((W2 * H2, 3), dtype=torch.uint8, device="cuda")
+    out = {"rgb8": rgb}
+    res = {}
+    for mode in ("refit", "rebuild"):
+        scene = crt.Scene(anim.mesh0)
+        scene.render(sc.camera, sc.light, W2, H2, spp, out=out, stream=stream)  # warm-up
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(frames)]
+        torch.cuda.synchronize()
+        for f in range(frames):
+            ev[f][0].record(stream)
+            scene.set_vertices(allv[f], rebuild=(mode == "rebuild" or f == 0), stream=stream)
+            ev[f][1].record(stream)
+            scene.render(sc.camera, sc.light, W2, H2, spp, out=out, stream=stream)
+            ev[f][2].record(stream)
+        torch.cuda.synchronize()
+        scene.check()
+        upd = [e[0].elapsed_time(e[1]) for e in ev[1:]]
+        frm = [e[0].elapsed_time(e[2]) for e in ev[1:]]
+        res[mode] = (float(np.mean(upd)), float(np.mean(frm)))
+        scene.close()
+    rays = W2 * H2 * spp
+    return {"frames": frames, "image": f"{W2}x{H2}x{spp}spp", "triangles": anim.mesh0.ntri,
+            "refit_update_ms": round(res["refit"][0], 4), "rebuild_update_ms": round(res["rebuild"][0], 4),
+            "refit_frame_ms": round(res["refit"][1], 3), "rebuild_frame_ms": round(res["rebuild"][1], 3),
+            "refit_mrays_s": round(rays / res["refit"][1] / 1e3, 1),
+            "rebuild_mrays_s": round(rays / res["rebuild"][1] / 1e3, 1)}
 
 
 def _cpu_impl():
@@ -313,6 +358,7 @@ def main():
     ap.add_argument("--impl", default="crt", choices=["crt", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the refit-vs-rebuild figures")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "crt" else args.warmup
     dist, rank, ws = dist_setup()

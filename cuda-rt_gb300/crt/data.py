@@ -24,7 +24,7 @@ import numpy as np
 
 __all__ = [
     "Mesh", "Camera", "Light", "Scene", "view_transform", "light_for", "soup", "icosphere",
-    "config0", "config1", "config2_frame", "config3", "config4", "lambert_material", "load_obj",
+    "config0", "config1", "config2_frame", "config3", "config4", "lambert_material", "load_obj", "Animation",
 ]
 
 
@@ -266,6 +266,39 @@ def config1(nu=224, width=1920, height=1080, spp=16) -> Scene:
     mesh = icosphere(nu, seed=1, cam_pos=cam_pos)
     return Scene(mesh, Camera(fov=60.0, focal_point=3.0, fstop=1.0 / (2 * 0.05)),
                  Light(position=light_for((3.0, 3.0, -3.0), cam_pos)), width, height, spp, "config1")
+
+
+class Animation:
+    """The refit workload's animated mesh: the large configuration's icosphere
+    with v_f = v_0 + 0.02 sin(2 pi f / frames + 5 x_0) n_0 (x_0, n_0 of the
+    rest pose, world space).  Frames are produced from float64 rest data, so
+    frame f always has the same float32 bytes."""
+
+    def __init__(self, nu=224, frames=60, seed=1, cam_pos=(0.0, 0.0, -3.0)):
+        rng = np.random.default_rng(seed)
+        u, tris = _geodesic(nu)
+        f = rng.uniform(1.0, 8.0, 4)
+        ph = rng.uniform(0.0, 2.0 * np.pi, 4)
+        ax = rng.normal(size=(4, 3))
+        ax /= np.linalg.norm(ax, axis=1, keepdims=True)
+        r = 1.0 + 0.05 * np.sin((u @ ax.T) * f[None] + ph[None]).sum(1)
+        self.v0 = u * r[:, None]
+        self.n0 = _vertex_normals(self.v0, tris)
+        self.tris = tris
+        self.frames = frames
+        self.cam_pos = cam_pos
+        nc = view_transform(self.n0, cam_pos, direction=True)
+        # frame 0 (its topology is the one the refit path keeps)
+        self.mesh0 = Mesh(self.vertices(0), tris, nc.astype(np.float32), tris.copy(),
+                          np.zeros(tris.shape[0], np.int32), lambert_material()[None])
+
+    def vertices(self, frame: int) -> np.ndarray:
+        v = self.v0 + (0.02 * np.sin(2.0 * np.pi * frame / self.frames + 5.0 * self.v0[:, 0]))[:, None] * self.n0
+        return view_transform(v, self.cam_pos).astype(np.float32)
+
+    def scene(self, width=1280, height=720, spp=4) -> Scene:
+        return Scene(self.mesh0, Camera(fov=60.0, focal_point=3.0, fstop=1.0 / (2 * 0.05)),
+                     Light(position=light_for((3.0, 3.0, -3.0), self.cam_pos)), width, height, spp, "config2")
 
 
 def config2_frame(frame: int, nu=224, width=1280, height=720, spp=4) -> Scene:
