@@ -60,7 +60,8 @@ class _RenderParams(C.Structure):
 
 class _RenderOut(C.Structure):
     _fields_ = [("rgb8", C.c_void_p), ("rgb_f32", C.c_void_p), ("hit_id", C.c_void_p), ("hit_t", C.c_void_p),
-                ("shadow", C.c_void_p), ("rays", C.c_void_p), ("traversal_stats", C.c_void_p)]
+                ("shadow", C.c_void_p), ("rays", C.c_void_p), ("traversal_stats", C.c_void_p),
+                ("rgb_f64", C.c_void_p), ("depth", C.c_void_p), ("shadow_id", C.c_void_p)]
 
 
 _lib = None
@@ -88,6 +89,8 @@ def lib():
             "crt_sort_pairs": [vp, vp, vp, vp, i32, i32, vp],
             "crt_sort_pairs_noalloc": [vp, vp, vp, vp, i32, i32, vp],
             "crt_scene_check": [vp, vp],
+            "crt_scene_set_materials": [vp, vp, i32, vp],
+            "crt_adjoint_lambert": [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -142,6 +145,7 @@ class Scene:
         mats = np.ascontiguousarray(np.asarray(mesh.materials, np.float64).reshape(-1, 16))
         self.ntri = int(mesh.vidx.shape[0])
         self.nv = int(mesh.verts.shape[0])
+        self.nmat = int(mats.shape[0])
         d = _MeshDesc(hold(mesh.verts, np.float32), self.nv, hold(mesh.normals, np.float32),
                       int(mesh.normals.shape[0]), hold(mesh.vidx, np.int32), hold(mesh.nidx, np.int32), self.ntri,
                       hold(mats, np.float64), int(mats.shape[0]), hold(mesh.matid, np.int32))
@@ -175,6 +179,25 @@ class Scene:
     def check(self, stream=None):
         _check(lib().crt_scene_check(self.h, _stream(stream)))
 
+    def set_materials(self, materials, stream=None):
+        """Replace the material table ((M, 16) float64: ka kd ks kt ke, shininess)."""
+        m = materials
+        if isinstance(m, np.ndarray):
+            m = np.ascontiguousarray(m, np.float64)
+        _check(lib().crt_scene_set_materials(self.h, _addr(m), int(m.shape[0]), _stream(stream)))
+
+    def adjoint(self, camera, light, width, height, spp, grad_rgb, grad_depth=None, out=None, stream=None):
+        """crt_adjoint_lambert: d loss / d (vertices, light position, kd) given
+        d loss / d rgb_f64 (and optionally d loss / d depth)."""
+        cam, lt, p = render_args(camera, light, width, height, spp, None)
+        if out is None:
+            out = dict(vertices=np.zeros((self.nv, 3), np.float64), light=np.zeros(3, np.float64),
+                       kd=np.zeros((self.nmat, 3), np.float64))
+        _check(lib().crt_adjoint_lambert(self.h, C.byref(cam), C.byref(lt), C.byref(p), _addr(grad_rgb),
+                                         _addr(grad_depth), _addr(out.get("vertices")), _addr(out.get("light")),
+                                         _addr(out.get("kd")), _stream(stream)))
+        return out
+
     def export(self) -> dict:
         n = self.ntri
         nn = max(2 * n - 1, 0)
@@ -204,7 +227,7 @@ class Scene:
         return (ids, t, nrm) if normals and not any_hit else (ids, t)
 
     def render(self, camera, light, width, height, spp, rows=None, out=None, aux=False, rays=False, rgbf=False,
-               stream=None):
+               rgbd=False, stream=None):
         """RayTracer::run + pullRaytracedImage.  Returns a dict of NumPy
         arrays unless `out` (a dict of preallocated buffers) is given."""
         cam, lt, p = render_args(camera, light, width, height, spp, rows)
@@ -213,13 +236,16 @@ class Scene:
             out = dict(rgb8=np.zeros((npx, 3), np.uint8))
             if rgbf:
                 out["rgb_f32"] = np.zeros((npx, 3), np.float32)
+            if rgbd:
+                out["rgb_f64"] = np.zeros((npx, 3), np.float64)
+                out["depth"] = np.zeros(npx, np.float64)
             if aux:
                 out.update(hit_id=np.zeros(ns, np.int32), hit_t=np.zeros(ns, np.float64),
-                           shadow=np.zeros(ns, np.int32))
+                           shadow=np.zeros(ns, np.int32), shadow_id=np.zeros(ns, np.int32))
             if rays:
                 out["rays"] = np.zeros((ns, 6), np.float64)
         o = _RenderOut(*[_addr(out.get(k)) for k in ("rgb8", "rgb_f32", "hit_id", "hit_t", "shadow", "rays",
-                                                     "traversal_stats")])
+                                                     "traversal_stats", "rgb_f64", "depth", "shadow_id")])
         _check(lib().crt_render(self.h, C.byref(cam), C.byref(lt), C.byref(p), C.byref(o), _stream(stream)))
         return out
 

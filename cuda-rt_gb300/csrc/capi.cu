@@ -407,7 +407,7 @@ crt_status crt_render(crt_scene* s, const crt_camera* cam, const crt_light* ligh
   a.latt[0] = light->constant_term, a.latt[1] = light->linear_term, a.latt[2] = light->quadratic_term;
   a.counter = s->counter;
   // outputs: whole-image buffers; a row band writes only its rows
-  DevView v8, vf, vh, vt, vs, vr, vst;
+  DevView v8, vf, vh, vt, vs, vr, vst, vd, vdp, vsi;
   const bool band = !(row0 == 0 && row1 == p->height);
   CRT_CUDA(v8.open(o->rgb8, 3 * npx, band, st), "stage rgb8");
   CRT_CUDA(vf.open(o->rgb_f32, 3 * sizeof(float) * npx, band, st), "stage rgb_f32");
@@ -416,6 +416,9 @@ crt_status crt_render(crt_scene* s, const crt_camera* cam, const crt_light* ligh
   CRT_CUDA(vs.open(o->shadow, sizeof(int32_t) * nsm, band, st), "stage shadow");
   CRT_CUDA(vr.open(o->rays, 6 * sizeof(double) * nsm, band, st), "stage rays");
   CRT_CUDA(vst.open(o->traversal_stats, 2 * sizeof(uint64_t), false, st), "stage stats");
+  CRT_CUDA(vd.open(o->rgb_f64, 3 * sizeof(double) * npx, band, st), "stage rgb_f64");
+  CRT_CUDA(vdp.open(o->depth, sizeof(double) * npx, band, st), "stage depth");
+  CRT_CUDA(vsi.open(o->shadow_id, sizeof(int32_t) * nsm, band, st), "stage shadow_id");
   if (vst.dev) CRT_CUDA(cudaMemsetAsync(vst.dev, 0, 2 * sizeof(uint64_t), st), "memset");
   a.rgb8 = static_cast<uint8_t*>(v8.dev);
   a.rgbf = static_cast<float*>(vf.dev);
@@ -424,8 +427,12 @@ crt_status crt_render(crt_scene* s, const crt_camera* cam, const crt_light* ligh
   a.shadow = static_cast<int*>(vs.dev);
   a.rays = static_cast<double*>(vr.dev);
   a.stats = static_cast<unsigned long long*>(vst.dev);
+  a.rgbd = static_cast<double*>(vd.dev);
+  a.depth = static_cast<double*>(vdp.dev);
+  a.shadow_id = static_cast<int*>(vsi.dev);
   CRT_CUDA(launch_render(dscene(s), a, st), "render launch");
-  const bool host_out = v8.temp || vf.temp || vh.temp || vt.temp || vs.temp || vr.temp || vst.temp;
+  const bool host_out = v8.temp || vf.temp || vh.temp || vt.temp || vs.temp || vr.temp || vst.temp || vd.temp ||
+                        vdp.temp || vsi.temp;
   CRT_CUDA(v8.close(true, st), "unstage");
   CRT_CUDA(vf.close(true, st), "unstage");
   CRT_CUDA(vh.close(true, st), "unstage");
@@ -433,8 +440,74 @@ crt_status crt_render(crt_scene* s, const crt_camera* cam, const crt_light* ligh
   CRT_CUDA(vs.close(true, st), "unstage");
   CRT_CUDA(vr.close(true, st), "unstage");
   CRT_CUDA(vst.close(true, st), "unstage");
+  CRT_CUDA(vd.close(true, st), "unstage");
+  CRT_CUDA(vdp.close(true, st), "unstage");
+  CRT_CUDA(vsi.close(true, st), "unstage");
   if (host_out) return check_globals(s, st);
   return CRT_OK;
+}
+
+crt_status crt_scene_set_materials(crt_scene* s, const crt_material* mats, int32_t num, void* stream) {
+  if (!s || !mats) return fail(CRT_INVALID_ARG, "null argument");
+  if (num != s->m.nmat) return fail(CRT_INVALID_ARG, "material count differs from the scene's");
+  CRT_CUDA(cudaMemcpyAsync(s->m.mats, mats, sizeof(DMat) * (size_t)num, cudaMemcpyDefault, S(stream)), "upload");
+  return CRT_OK;
+}
+
+crt_status crt_adjoint_lambert(crt_scene* s, const crt_camera* cam, const crt_light* light,
+                               const crt_render_params* p, const double* grad_rgb, const double* grad_depth,
+                               double* grad_vertices, double* grad_light, double* grad_kd, void* stream) {
+  if (!s || !cam || !light || !p || !grad_rgb) return fail(CRT_INVALID_ARG, "null argument");
+  if (!s->built) return fail(CRT_NOT_BUILT, "no BVH");
+  if (p->width <= 0 || p->height <= 0 || p->spp <= 0) return fail(CRT_INVALID_ARG, "width, height, spp must be > 0");
+  if ((int64_t)p->width * p->height > (int64_t)1 << 30) return fail(CRT_INVALID_ARG, "image too large");
+  int row0 = p->row_begin, row1 = p->row_end;
+  if (row0 == 0 && row1 == 0) row1 = p->height;
+  if (row0 < 0 || row1 > p->height || row0 >= row1) return fail(CRT_INVALID_ARG, "bad row range");
+  cudaStream_t st = S(stream);
+  const size_t npx = (size_t)p->width * p->height;
+  RenderArgs a;
+  a.W = p->width, a.H = p->height, a.spp = p->spp, a.row0 = row0, a.row1 = row1;
+  a.angle = std::tan(M_PI * 0.5 * cam->fov / 180.0f);
+  a.aspect = double(p->width) / double(p->height);
+  a.invW = 1.0 / double(p->width);
+  a.invH = 1.0 / double(p->height);
+  a.aperture = 1 / cam->fstop;
+  a.focal = cam->focal_point;
+  for (int k = 0; k < 3; k++) {
+    a.eye[k] = cam->eye[k];
+    a.lpos[k] = light->position[k];
+    a.lcol[k] = light->color[k];
+  }
+  a.lradius = light->radius;
+  a.latt[0] = light->constant_term, a.latt[1] = light->linear_term, a.latt[2] = light->quadratic_term;
+  a.counter = s->counter;
+  a.rgb8 = nullptr, a.rgbf = nullptr, a.hit_id = nullptr, a.hit_t = nullptr, a.shadow = nullptr, a.rays = nullptr;
+  a.stats = nullptr;
+  DevView vg, vgd, vv, vl, vk;
+  CRT_CUDA(vg.open(const_cast<double*>(grad_rgb), 3 * sizeof(double) * npx, true, st), "stage grad_rgb");
+  CRT_CUDA(vgd.open(const_cast<double*>(grad_depth), sizeof(double) * npx, true, st), "stage grad_depth");
+  // gradient outputs: always through device scratch (they are accumulated atomically)
+  const size_t nv3 = 3 * (size_t)s->m.nv, nk3 = 3 * (size_t)s->m.nmat;
+  double* acc = nullptr;
+  CRT_CUDA(cudaMallocAsync(&acc, sizeof(double) * (nv3 + 3 + nk3), st), "scratch");
+  CRT_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * (nv3 + 3 + nk3), st), "memset");
+  a.grad_rgb = static_cast<const double*>(vg.dev);
+  a.grad_depth = static_cast<const double*>(vgd.dev);
+  a.grad_verts = acc;
+  a.grad_light = acc + nv3;
+  a.grad_albedo = acc + nv3 + 3;
+  CRT_CUDA(launch_render(dscene(s), a, st), "adjoint launch");
+  auto out = [&](double* dst, const double* src, size_t n) -> cudaError_t {
+    return (dst && n) ? cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDefault, st) : cudaSuccess;
+  };
+  CRT_CUDA(out(grad_vertices, acc, nv3), "download");
+  CRT_CUDA(out(grad_light, acc + nv3, 3), "download");
+  CRT_CUDA(out(grad_kd, acc + nv3 + 3, nk3), "download");
+  CRT_CUDA(cudaFreeAsync(acc, st), "free");
+  CRT_CUDA(vg.close(false, st), "unstage");
+  CRT_CUDA(vgd.close(false, st), "unstage");
+  return check_globals(s, st);
 }
 
 crt_status crt_morton(const float* verts, const int32_t* vidx, int32_t n, const float* box6, int32_t* codes,

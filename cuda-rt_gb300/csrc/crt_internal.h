@@ -68,6 +68,15 @@ struct RenderArgs {
   double* rays;
   unsigned* counter;
   unsigned long long* stats;  // optional [2]: internal nodes visited, triangles tested
+  double* rgbd = nullptr;     // optional: mean colour in double
+  double* depth = nullptr;    // optional: mean hit t (misses count 0)
+  int* shadow_id = nullptr;   // optional: occluding triangle per sample, -1 if none
+  // adjoint (grad_rgb != NULL selects it)
+  const double* grad_rgb = nullptr;
+  const double* grad_depth = nullptr;
+  double* grad_verts = nullptr;
+  double* grad_light = nullptr;
+  double* grad_albedo = nullptr;
 };
 cudaError_t launch_render(const DScene& S, const RenderArgs& a, cudaStream_t st);
 cudaError_t launch_trace(const DScene& S, const double* rays, int64_t n, bool any, int* ids, double* t,

@@ -2,13 +2,13 @@
 //
 // k_trace<ANY>  closest hit (BVH_d::intersect) or first hit in left-first
 //               DFS order (BVH_d::intersectAny) for a batch of double rays.
-// k_render      runRayTracerKernelRec (kernels/raytracer.cu:95-166) with
+// k_pixels      runRayTracerKernelRec (kernels/raytracer.cu:95-166) with
 //               traceRay (raytracer.cu:169-249), Material::shade
 //               (kernels/material.cu:6-40) and the positional Light
-//               (kernels/Light.cu:5-86).  Persistent: each warp claims
-//               8x4-pixel tiles from a counter, one pixel per lane; a lane
-//               runs its pixel's samples in order because the mrand stream
-//               couples them (a hit consumes three extra draws).
+//               (kernels/Light.cu:5-86); also its adjoint.  Persistent: each
+//               warp claims 8x4-pixel tiles from a counter, one pixel per
+//               lane; a lane runs its pixel's samples in order because the
+//               mrand stream couples them (a hit consumes three extra draws).
 #include "crt_internal.h"
 
 namespace crt {
@@ -38,14 +38,26 @@ __global__ void __launch_bounds__(128) k_trace(DScene S, const double* __restric
   }
 }
 
-__device__ __forceinline__ DMat load_mat(const DScene& S, int tri) {
-  return S.mats[__ldg(S.matid + tri)];
-}
-
 constexpr int kTileW = 8, kTileH = 4;
 
-template <bool STATS>
-__global__ void __launch_bounds__(128, 4) k_render(DScene S, RenderArgs A) {
+enum PixelMode { kRender = 0, kRenderStats = 1, kAdjoint = 2 };
+
+// Warp-reduced atomic add of a double (light gradient: few addresses).
+__device__ __forceinline__ void warp_add(double* dst, double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(dst, v);
+}
+
+// runRayTracerKernelRec (kernels/raytracer.cu:95-166) per pixel, with
+// traceRay (raytracer.cu:169-249), Material::shade (kernels/material.cu:6-40)
+// and the positional Light (kernels/Light.cu:5-86).  MODE kAdjoint re-runs the
+// same samples (same rays, hits and shadow tests: nothing is stored between
+// the forward and the adjoint) and accumulates d loss / d (vertices, light
+// position, albedo) for the Lambert and distance terms; visibility (which
+// triangle is hit, whether the shadow ray is blocked) is held fixed.
+template <int MODE>
+__global__ void __launch_bounds__(128, 4) k_pixels(DScene S, RenderArgs A) {
   TravStats ts;
   float rb[6], B, D;
   scene_consts(S, rb, B, D);
@@ -55,6 +67,7 @@ __global__ void __launch_bounds__(128, 4) k_render(DScene S, RenderArgs A) {
   const int ntiles = tiles_x * tiles_y;
   const int gx = (A.W + 15) / 16;  // gridDim.x of the reference's 16x16 launch
   const D3 lpos = d3(A.lpos[0], A.lpos[1], A.lpos[2]);
+  D3 glight = d3(0, 0, 0);
   while (true) {
     int tile = 0;
     if (lane == 0) tile = (int)atomicAdd(A.counter, 1u);
@@ -71,6 +84,15 @@ __global__ void __launch_bounds__(128, 4) k_render(DScene S, RenderArgs A) {
     const double xx = (2 * ((px + 0.5) * A.invW) - 1) * A.angle * A.aspect;
     const double yy = (1 - 2 * ((py + 0.5) * A.invH)) * A.angle;
     D3 acc = d3(0, 0, 0);
+    double depth = 0.0;
+    D3 G = d3(0, 0, 0);
+    double Gd = 0.0;
+    if (MODE == kAdjoint) {
+      const double inv = 1.0 / (double)A.spp;
+      G = d3(A.grad_rgb[3 * (int64_t)idx] * inv, A.grad_rgb[3 * (int64_t)idx + 1] * inv,
+             A.grad_rgb[3 * (int64_t)idx + 2] * inv);
+      Gd = A.grad_depth ? A.grad_depth[idx] * inv : 0.0;
+    }
     for (int k = 0; k < A.spp; k++) {
       const int64_t si = (int64_t)idx * A.spp + k;
       const double dofAngle = 2 * 3.14159265358979323846 * rand_double(st);
@@ -82,50 +104,67 @@ __global__ void __launch_bounds__(128, 4) k_render(DScene S, RenderArgs A) {
       D3 dir = normalize_exact(d3(xx, yy, -1.0));
       dir = d3(dir.x * A.focal, dir.y * A.focal, dir.z * A.focal) - org;
       dir = normalize_exact(dir);
-      if (A.rays) {
+      if (MODE != kAdjoint && A.rays) {
         double* rr = A.rays + 6 * si;
         rr[0] = org.x, rr[1] = org.y, rr[2] = org.z, rr[3] = dir.x, rr[4] = dir.y, rr[5] = dir.z;
       }
       RayC rc;
       ray_setup(rc, org.x, org.y, org.z, dir.x, dir.y, dir.z, B, D);
       HitRec h;
-      const int res = traverse<false, STATS>(S, rc, rb, h, &ts);
+      const int res = traverse<false, MODE == kRenderStats>(S, rc, rb, h, &ts);
       if (res < 0) atomicOr(&S.g->err, kErrStack);
       D3 col;
-      int sh = -1;
+      int sh = -1, shid = -1;
       if (res > 0) {
         const D3 q = org + (h.t * dir);
-        const DMat m = load_mat(S, h.id);
-        const D3 N = hit_normal(S, h);
+        const int mid = __ldg(S.matid + h.id);
+        const DMat m = S.mats[mid];
+        // smooth normal, bvh.cu:357-364 (hit_normal, kept apart for the adjoint)
+        const int na = S.nidx[3 * h.id], nb = S.nidx[3 * h.id + 1], nc = S.nidx[3 * h.id + 2];
+        const D3 nA = d3(S.normals[3 * na], S.normals[3 * na + 1], S.normals[3 * na + 2]);
+        const D3 nB = d3(S.normals[3 * nb], S.normals[3 * nb + 1], S.normals[3 * nb + 2]);
+        const D3 nC = d3(S.normals[3 * nc], S.normals[3 * nc + 1], S.normals[3 * nc + 2]);
+        const D3 Nr = (1.0 - (h.alpha + h.beta)) * nA + h.alpha * nB + h.beta * nC;
+        const double sN = 1.0 / (double)sqrtf(__double2float_rn(Nr.x * Nr.x + Nr.y * Nr.y + Nr.z * Nr.z));
+        const D3 N = d3(Nr.x * sN, Nr.y * sN, Nr.z * sN);
         D3 I = d3(m.ke[0] + m.ka[0] * 0.0, m.ke[1] + m.ka[1] * 0.0, m.ke[2] + m.ka[2] * 0.0);
         D3 V = d3(A.eye[0], A.eye[1], A.eye[2]) - q;
         V = normalize_exact(d3(-V.x, -V.y, -V.z));
         // Light::getDirection: three draws (x, y, z), times radius, minus 0.5
         const double r0 = rand_double(st), r1 = rand_double(st), r2 = rand_double(st);
         const D3 off = d3(r0 * A.lradius - 0.5, r1 * A.lradius - 0.5, r2 * A.lradius - 0.5);
-        const D3 L = normalize_exact(lpos + off - q);
+        const D3 Lp = lpos + off - q;
+        const double sL = 1.0 / (double)sqrtf(__double2float_rn(Lp.x * Lp.x + Lp.y * Lp.y + Lp.z * Lp.z));
+        const D3 L = d3(Lp.x * sL, Lp.y * sL, Lp.z * sL);
         // Light::distanceAttenuation
         const double dist = norm_exact(lpos - q);
         double fall = A.latt[0] + (A.latt[1] + A.latt[2] * dist) * dist;
-        fall = (fabs(fall) < kRayEps) ? 1.0 : 1.0 / fall;
+        const bool tiny = fabs(fall) < kRayEps;
+        fall = tiny ? 1.0 : 1.0 / fall;
         const double datt = fmin(1.0, fall);
         // Light::shadowAttenuation: any-hit from q towards the light
         D3 satt = d3(1, 1, 1);
         RayC sr;
         ray_setup(sr, q.x, q.y, q.z, L.x, L.y, L.z, B, D);
         HitRec s;
-        const int sres = traverse<true, STATS>(S, sr, rb, s, &ts);
+        const int sres = traverse<true, MODE == kRenderStats>(S, sr, rb, s, &ts);
         if (sres < 0) atomicOr(&S.g->err, kErrStack);
         sh = 0;
+        int omid = -1;
+        bool otrans = false;
+        DMat om;
         if (sres > 0 && s.t < norm_exact(lpos - q) && !(s.t < kRayEps)) {
           sh = 1;
-          const DMat om = load_mat(S, s.id);
-          const bool trans = om.kt[0] == 0 && om.kt[1] == 0 && om.kt[2] == 0;  // Trans() = isZero(kt)
-          satt = trans ? d3(om.kd[0] * (1 - om.kt[0]), om.kd[1] * (1 - om.kt[1]), om.kd[2] * (1 - om.kt[2]))
-                       : d3(0, 0, 0);
+          shid = s.id;
+          omid = __ldg(S.matid + s.id);
+          om = S.mats[omid];
+          otrans = om.kt[0] == 0 && om.kt[1] == 0 && om.kt[2] == 0;  // Trans() = isZero(kt)
+          satt = otrans ? d3(om.kd[0] * (1 - om.kt[0]), om.kd[1] * (1 - om.kt[1]), om.kd[2] * (1 - om.kt[2]))
+                        : d3(0, 0, 0);
         }
         const D3 att = datt * satt;
-        double lam = dot(N, L);
+        const double NL = dot(N, L);
+        double lam = NL;
         if (lam < 0) lam = 0;
         const D3 diffuse = d3(m.kd[0] * lam, m.kd[1] * lam, m.kd[2] * lam);
         D3 R = (-2.0 * dot(L, N)) * N + L;
@@ -136,14 +175,83 @@ __global__ void __launch_bounds__(128, 4) k_render(DScene S, RenderArgs A) {
         const D3 ds = diffuse + spec;
         I = I + d3(att.x * ds.x * A.lcol[0], att.y * ds.y * A.lcol[1], att.z * ds.z * A.lcol[2]);
         col = I;
+        if (MODE == kAdjoint) {
+          const double Gc[3] = {G.x, G.y, G.z};
+          const double sa[3] = {satt.x, satt.y, satt.z};
+          const double dsv[3] = {ds.x, ds.y, ds.z};
+          double S_lam = 0.0, gdatt = 0.0;
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            const double w = Gc[c] * A.lcol[c];
+            // d/d kd of the hit triangle's material (Lambert term)
+            const double gkd = w * datt * sa[c] * lam;
+            if (gkd != 0.0) atomicAdd(A.grad_albedo + 3 * mid + c, gkd);
+            // d/d kd of an opaque occluder's material: the reference's shadow
+            // attenuation is kd % (1 - kt) of the occluder (Light.cu:22-24)
+            if (sh == 1 && otrans) {
+              const double go = w * datt * dsv[c] * (1 - om.kt[c]);
+              if (go != 0.0) atomicAdd(A.grad_albedo + 3 * omid + c, go);
+            }
+            S_lam += w * datt * sa[c] * m.kd[c];
+            gdatt += w * sa[c] * dsv[c];
+          }
+          if (!(NL > 0)) S_lam = 0.0;  // lam = max(N.L, 0)
+          // datt = min(1, 1/fall(dist)), fall = a + (b + c dist) dist
+          double gdist = 0.0;
+          if (!tiny && fall < 1.0) {
+            const double fr = 1.0 / fall;  // the falloff polynomial itself
+            gdist = gdatt * (-(A.latt[1] + 2.0 * A.latt[2] * dist) / (fr * fr));
+          }
+          // lam through L = Lp / |Lp|, Lp = P + off - q
+          const D3 gLp = d3((N.x - NL * L.x) * sL * S_lam, (N.y - NL * L.y) * sL * S_lam,
+                            (N.z - NL * L.z) * sL * S_lam);
+          const D3 u = (dist > 0.0) ? (1.0 / dist) * (lpos - q) : d3(0, 0, 0);
+          const D3 gP = gLp + gdist * u;
+          glight = glight + gP;
+          const D3 gq = d3(-gP.x, -gP.y, -gP.z);
+          // lam through N = Nr / |Nr|, Nr = (1-a-b) nA + a nB + b nC
+          const D3 gN = d3((L.x - NL * N.x) * sN * S_lam, (L.y - NL * N.y) * sN * S_lam,
+                           (L.z - NL * N.z) * sN * S_lam);
+          const double g_al = dot(gN, nB - nA), g_be = dot(gN, nC - nA);
+          const double g_t = dot(gq, dir) + Gd;  // q = o + t d, and the depth output
+          // (t, alpha, beta) solve [-d | E1 | E2] x = o - A; moving the hit's
+          // barycentric point by delta moves x by -M^-1 delta, so
+          // d loss / d delta = -M^-T g, split over A, B, C by (1-a-b, a, b).
+          const int ia = S.vidx[3 * h.id], ib = S.vidx[3 * h.id + 1], ic = S.vidx[3 * h.id + 2];
+          const D3 Av = d3(S.verts[3 * ia], S.verts[3 * ia + 1], S.verts[3 * ia + 2]);
+          const D3 Bv = d3(S.verts[3 * ib], S.verts[3 * ib + 1], S.verts[3 * ib + 2]);
+          const D3 Cv = d3(S.verts[3 * ic], S.verts[3 * ic + 1], S.verts[3 * ic + 2]);
+          const D3 ma = d3(-dir.x, -dir.y, -dir.z), mb = Bv - Av, mc = Cv - Av;
+          const D3 bc = d3(mb.y * mc.z - mb.z * mc.y, mb.z * mc.x - mb.x * mc.z, mb.x * mc.y - mb.y * mc.x);
+          const D3 ca = d3(mc.y * ma.z - mc.z * ma.y, mc.z * ma.x - mc.x * ma.z, mc.x * ma.y - mc.y * ma.x);
+          const D3 ab = d3(ma.y * mb.z - ma.z * mb.y, ma.z * mb.x - ma.x * mb.z, ma.x * mb.y - ma.y * mb.x);
+          const double det = dot(ma, bc);
+          if (det != 0.0) {
+            const double id = -1.0 / det;
+            const D3 w = d3(id * (g_t * bc.x + g_al * ca.x + g_be * ab.x), id * (g_t * bc.y + g_al * ca.y + g_be * ab.y),
+                            id * (g_t * bc.z + g_al * ca.z + g_be * ab.z));
+            const double wa = 1.0 - (h.alpha + h.beta), wb = h.alpha, wc = h.beta;
+            atomicAdd(A.grad_verts + 3 * ia, wa * w.x), atomicAdd(A.grad_verts + 3 * ia + 1, wa * w.y);
+            atomicAdd(A.grad_verts + 3 * ia + 2, wa * w.z);
+            atomicAdd(A.grad_verts + 3 * ib, wb * w.x), atomicAdd(A.grad_verts + 3 * ib + 1, wb * w.y);
+            atomicAdd(A.grad_verts + 3 * ib + 2, wb * w.z);
+            atomicAdd(A.grad_verts + 3 * ic, wc * w.x), atomicAdd(A.grad_verts + 3 * ic + 1, wc * w.y);
+            atomicAdd(A.grad_verts + 3 * ic + 2, wc * w.z);
+          }
+        }
+        depth += h.t;
       } else {
         col = d3(0.9, 0.9, 0.9);
       }
       acc = acc + col;
-      if (A.hit_id) A.hit_id[si] = res > 0 ? h.id : -1;
-      if (A.hit_t) A.hit_t[si] = res > 0 ? h.t : 0.0;
-      if (A.shadow) A.shadow[si] = sh;
+      if (MODE != kAdjoint) {
+        if (A.hit_id) A.hit_id[si] = res > 0 ? h.id : -1;
+        if (A.hit_t) A.hit_t[si] = res > 0 ? h.t : 0.0;
+        if (A.shadow) A.shadow[si] = sh;
+        if (A.shadow_id) A.shadow_id[si] = shid;
+      }
     }
+    if (MODE == kAdjoint) continue;
     const double inv = (double)A.spp;
     acc = d3(acc.x / inv, acc.y / inv, acc.z / inv);
     if (A.rgbf) {
@@ -151,6 +259,12 @@ __global__ void __launch_bounds__(128, 4) k_render(DScene S, RenderArgs A) {
       A.rgbf[3 * (int64_t)idx + 1] = (float)acc.y;
       A.rgbf[3 * (int64_t)idx + 2] = (float)acc.z;
     }
+    if (A.rgbd) {
+      A.rgbd[3 * (int64_t)idx] = acc.x;
+      A.rgbd[3 * (int64_t)idx + 1] = acc.y;
+      A.rgbd[3 * (int64_t)idx + 2] = acc.z;
+    }
+    if (A.depth) A.depth[idx] = depth / inv;
     if (A.rgb8) {
       const double cc[3] = {acc.x, acc.y, acc.z};
 #pragma unroll
@@ -162,7 +276,7 @@ __global__ void __launch_bounds__(128, 4) k_render(DScene S, RenderArgs A) {
       }
     }
   }
-  if (STATS) {
+  if (MODE == kRenderStats) {
     unsigned long long a = ts.nodes, b = ts.tris;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -174,6 +288,11 @@ __global__ void __launch_bounds__(128, 4) k_render(DScene S, RenderArgs A) {
       atomicAdd(A.stats + 1, b);
     }
   }
+  if (MODE == kAdjoint) {
+    warp_add(A.grad_light, glight.x);
+    warp_add(A.grad_light + 1, glight.y);
+    warp_add(A.grad_light + 2, glight.z);
+  }
 }
 
 }  // namespace
@@ -181,12 +300,15 @@ __global__ void __launch_bounds__(128, 4) k_render(DScene S, RenderArgs A) {
 cudaError_t launch_render(const DScene& S, const RenderArgs& a, cudaStream_t st) {
   cudaMemsetAsync(a.counter, 0, sizeof(unsigned), st);
   int bps = 0;
-  if (a.stats) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_render<true>, 128, 0);
-    k_render<true><<<num_sms() * (bps > 0 ? bps : 1), 128, 0, st>>>(S, a);
+  if (a.grad_rgb) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_pixels<kAdjoint>, 128, 0);
+    k_pixels<kAdjoint><<<num_sms() * (bps > 0 ? bps : 1), 128, 0, st>>>(S, a);
+  } else if (a.stats) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_pixels<kRenderStats>, 128, 0);
+    k_pixels<kRenderStats><<<num_sms() * (bps > 0 ? bps : 1), 128, 0, st>>>(S, a);
   } else {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_render<false>, 128, 0);
-    k_render<false><<<num_sms() * (bps > 0 ? bps : 1), 128, 0, st>>>(S, a);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_pixels<kRender>, 128, 0);
+    k_pixels<kRender><<<num_sms() * (bps > 0 ? bps : 1), 128, 0, st>>>(S, a);
   }
   return cudaGetLastError();
 }

@@ -105,6 +105,9 @@ typedef struct crt_render_out {
   double* rays;      /* (idx*spp + k)*6: primary ray origin, direction */
   uint64_t* traversal_stats; /* [2]: internal nodes visited, triangles tested (all
                                 rays of the call); non-NULL selects an instrumented kernel */
+  double* rgb_f64;   /* idx*3: mean colour before clamping, in double */
+  double* depth;     /* idx: mean over samples of the hit t (a miss counts 0) */
+  int32_t* shadow_id; /* idx*spp + k: the occluding triangle when shadow is 1, else -1 */
 } crt_render_out;
 
 /* ---- scene lifetime: Scene_d::operator=(const Scene_h&) (src/scene.cpp:82-160)
@@ -151,6 +154,26 @@ crt_status crt_trace_shadow(crt_scene* scene, const double* rays, int64_t n, int
  * samples, clamp, quantise. */
 crt_status crt_render(crt_scene* scene, const crt_camera* camera, const crt_light* light,
                       const crt_render_params* params, const crt_render_out* out, void* stream);
+
+/* Replace the material table (same count as at creation), e.g. new
+ * per-triangle albedos.  Asynchronous. */
+crt_status crt_scene_set_materials(crt_scene* scene, const crt_material* materials, int32_t num_materials,
+                                   void* stream);
+
+/* ---- differentiation (no counterpart in the reference): the adjoint of
+ * crt_render's mean colour (rgb_f64) and depth with respect to the vertex
+ * positions, the light position and each material's kd, for Lambert shading
+ * with distance attenuation.  Interior gradients only: which triangle each
+ * sample hits and whether its shadow ray is blocked are held fixed (no
+ * visibility edges); the specular term is treated as constant.  The samples
+ * are recomputed per tile (same rays, hits and shadow tests as the forward),
+ * nothing is stored between the two.  Inputs: grad_rgb[W*H*3] = d loss /
+ * d rgb_f64, grad_depth[W*H] = d loss / d depth (may be NULL).  Outputs are
+ * overwritten: grad_vertices[num_vertices*3], grad_light[3],
+ * grad_kd[num_materials*3] (any may be NULL).  Host or device pointers. */
+crt_status crt_adjoint_lambert(crt_scene* scene, const crt_camera* camera, const crt_light* light,
+                               const crt_render_params* params, const double* grad_rgb, const double* grad_depth,
+                               double* grad_vertices, double* grad_light, double* grad_kd, void* stream);
 
 /* ---- stage-level entry points (device pointers only, asynchronous) ----
  * Morton codes of each triangle's centroid (computeMortonCodesKernel,

@@ -532,13 +532,14 @@ int orc_trace(void* h, const double* rays, int n, int any, int* ids, double* t, 
 //   hit_t[idx*spp + k]    its t (optional)
 //   shadow[idx*spp + k]   1 if the shadow ray's first hit occluded the light,
 //                         0 if lit, -1 if the primary ray missed (optional)
+//   shadow_id[idx*spp+k]  the occluding triangle when shadow is 1, else -1 (optional)
 //   rays_out[(idx*spp+k)*6]  the primary ray (optional)
 // rays_in (optional) replaces the generated primary ray of every sample; the
 // random draws are still consumed as in the reference.
 // Returns the number of stack overflows.
 int orc_render(void* h, const orc_camera* cam, const orc_light* light, int W, int H, int spp, int row0,
                int row1, uint8_t* rgb8, double* color, int* hit_id, double* hit_t, int* shadow,
-               const double* rays_in, double* rays_out, int nthreads) {
+               const double* rays_in, double* rays_out, int nthreads, int* shadow_id) {
   const Scene* s = (const Scene*)h;
   const int gx = (W + 15) / 16;  // gridDim.x of the 16x16 launch (raytracer.cu:56-58)
   int overflow = 0;
@@ -585,7 +586,7 @@ int orc_render(void* h, const orc_camera* cam, const orc_light* light, int W, in
         int res = traverse(*s, org, dir, false, &hh);
         if (res < 0) overflow++;
         V3 col;
-        int sh = -1;
+        int sh = -1, shid = -1;
         if (res > 0) {
           V3 q = org + (hh.t * dir);
           const Material& m = s->mats[s->matid[hh.id]];
@@ -620,6 +621,7 @@ int orc_render(void* h, const orc_camera* cam, const orc_light* light, int W, in
               satt = v3(1, 1, 1);
             } else {
               sh = 1;
+              shid = sh_hit.id;
               // Trans() is isZero(kt) (inc/material.h:31), so an opaque
               // occluder (kt = 0) passes kd % (1 - kt).
               bool trans = om.kt[0] == 0 && om.kt[1] == 0 && om.kt[2] == 0;
@@ -647,6 +649,7 @@ int orc_render(void* h, const orc_camera* cam, const orc_light* light, int W, in
         if (hit_id) hit_id[si] = res > 0 ? hh.id : -1;
         if (hit_t) hit_t[si] = res > 0 ? hh.t : 0.0;
         if (shadow) shadow[si] = sh;
+        if (shadow_id) shadow_id[si] = shid;
       }
       acc = v3(acc.x / double(spp), acc.y / double(spp), acc.z / double(spp));
       if (color) {
@@ -664,6 +667,131 @@ int orc_render(void* h, const orc_camera* cam, const orc_light* light, int W, in
     }
   }
   return overflow;
+}
+
+// Adjoint of the mean colour (and mean hit t) of orc_render with respect to
+// the vertices, the light position and each material's kd: the float64
+// reference for the GPU adjoint (no counterpart in the reference).  The
+// samples are regenerated exactly as in orc_render; which triangle is hit and
+// whether the shadow ray is blocked are held fixed, the specular term is
+// treated as constant, and the float roundings inside normalize()/norm() are
+// taken as exact scalings.  grad_rgb[idx*3], grad_depth[idx] (may be NULL);
+// outputs are accumulated into grad_v[V*3], grad_light[3], grad_kd[M*3].
+void orc_adjoint(void* h, const orc_camera* cam, const orc_light* light, int W, int H, int spp,
+                 const double* grad_rgb, const double* grad_depth, double* grad_v, double* grad_light,
+                 double* grad_kd, int nthreads) {
+  const Scene* s = (const Scene*)h;
+  const int gx = (W + 15) / 16;
+  const double invW = 1.0 / double(W), invH = 1.0 / double(H);
+  const double aspect = double(W) / double(H);
+  const double angle = tan(M_PI * 0.5 * cam->fov / 180.0f);
+  const double aperture = 1 / cam->fstop;
+  const V3 lpos = v3(light->position[0], light->position[1], light->position[2]);
+  const double lcol[3] = {light->color[0], light->color[1], light->color[2]};
+  auto add = [](double* p, double v) {
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+    *p += v;
+  };
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+  for (int py = 0; py < H; py++) {
+    for (int px = 0; px < W; px++) {
+      const int idx = (H - py - 1) * W + px;
+      uint32_t g = (uint32_t)(((py / 16) * gx + px / 16) * 256 + (py % 16) * 16 + (px % 16));
+      uint32_t st = wang_hash(g);
+      double xx = (2 * ((px + 0.5) * invW) - 1) * angle * aspect;
+      double yy = (1 - 2 * ((py + 0.5) * invH)) * angle;
+      const double G[3] = {grad_rgb[3 * (size_t)idx] / spp, grad_rgb[3 * (size_t)idx + 1] / spp,
+                           grad_rgb[3 * (size_t)idx + 2] / spp};
+      const double Gd = grad_depth ? grad_depth[idx] / spp : 0.0;
+      for (int k = 0; k < spp; k++) {
+        double dofAngle = 2 * M_PI * rand_double(st);
+        double dofRadius = aperture * sqrt(rand_double(st)) / 2.0;
+        V3 org = v3(dofRadius * cos(dofAngle), dofRadius * sin(dofAngle), 0);
+        V3 dir = normalize(v3(xx, yy, -1.0)) * cam->focal_point - org;
+        dir = normalize(dir);
+        Hit hh;
+        if (traverse(*s, org, dir, false, &hh) <= 0) continue;
+        V3 q = org + (hh.t * dir);
+        const int mid = s->matid[hh.id];
+        const Material& m = s->mats[mid];
+        V3 nA = s->normals[s->nidx[3 * hh.id]], nB = s->normals[s->nidx[3 * hh.id + 1]],
+           nC = s->normals[s->nidx[3 * hh.id + 2]];
+        V3 Nr = (1.0 - (hh.alpha + hh.beta)) * nA + hh.alpha * nB + hh.beta * nC;
+        double sN = 1.0 / (double)sqrtf((float)(Nr.x * Nr.x + Nr.y * Nr.y + Nr.z * Nr.z));
+        V3 N = Nr * sN;
+        double r0 = rand_double(st), r1 = rand_double(st), r2 = rand_double(st);
+        V3 off = v3(r0 * light->radius - 0.5, r1 * light->radius - 0.5, r2 * light->radius - 0.5);
+        V3 Lp = lpos + off - q;
+        double sL = 1.0 / (double)sqrtf((float)(Lp.x * Lp.x + Lp.y * Lp.y + Lp.z * Lp.z));
+        V3 L = Lp * sL;
+        double dist = norm(lpos - q);
+        double fall = light->constant_term + (light->linear_term + light->quadratic_term * dist) * dist;
+        bool tiny = fabs(fall) < kRayEps;
+        fall = tiny ? 1.0 : 1.0 / fall;
+        double datt = fmin(1.0, fall);
+        double satt[3] = {1, 1, 1};
+        Hit sh;
+        int omid = -1;
+        bool otrans = false;
+        if (traverse(*s, q, L, true, &sh) > 0 && sh.t < norm(lpos - q) && !(sh.t < kRayEps)) {
+          omid = s->matid[sh.id];
+          const Material& om = s->mats[omid];
+          otrans = om.kt[0] == 0 && om.kt[1] == 0 && om.kt[2] == 0;
+          for (int c = 0; c < 3; c++) satt[c] = otrans ? om.kd[c] * (1 - om.kt[c]) : 0.0;
+        }
+        double NL = dot(N, L);
+        double lam = NL < 0 ? 0 : NL;
+        // specular value (constant for the gradient)
+        V3 Vv = v3(cam->eye[0], cam->eye[1], cam->eye[2]) - q;
+        Vv = normalize(v3(-Vv.x, -Vv.y, -Vv.z));
+        V3 R = normalize((-2.0 * dot(L, N)) * N + L);
+        double sp = (double)powf((float)fmax(0.0, dot(R, Vv)), (float)m.shininess);
+        double S_lam = 0.0, gdatt = 0.0;
+        for (int c = 0; c < 3; c++) {
+          double w = G[c] * lcol[c];
+          double dsv = m.kd[c] * lam + m.ks[c] * sp;
+          add(grad_kd + 3 * mid + c, w * datt * satt[c] * lam);
+          if (omid >= 0 && otrans) add(grad_kd + 3 * omid + c, w * datt * dsv * (1 - s->mats[omid].kt[c]));
+          S_lam += w * datt * satt[c] * m.kd[c];
+          gdatt += w * satt[c] * dsv;
+        }
+        if (!(NL > 0)) S_lam = 0.0;
+        double gdist = 0.0;
+        if (!tiny && fall < 1.0) {
+          double fr = 1.0 / fall;
+          gdist = gdatt * (-(light->linear_term + 2.0 * light->quadratic_term * dist) / (fr * fr));
+        }
+        V3 gLp = v3((N.x - NL * L.x) * sL * S_lam, (N.y - NL * L.y) * sL * S_lam, (N.z - NL * L.z) * sL * S_lam);
+        V3 u = dist > 0 ? (1.0 / dist) * (lpos - q) : v3(0, 0, 0);
+        V3 gP = gLp + gdist * u;
+        for (int c = 0; c < 3; c++) add(grad_light + c, comp(gP, c));
+        V3 gq = v3(-gP.x, -gP.y, -gP.z);
+        V3 gN = v3((L.x - NL * N.x) * sN * S_lam, (L.y - NL * N.y) * sN * S_lam, (L.z - NL * N.z) * sN * S_lam);
+        double g_al = dot(gN, nB - nA), g_be = dot(gN, nC - nA);
+        double g_t = dot(gq, dir) + Gd;
+        const int ia = s->vidx[3 * hh.id], ib = s->vidx[3 * hh.id + 1], ic = s->vidx[3 * hh.id + 2];
+        V3 A = s->verts[ia], Bv = s->verts[ib], Cv = s->verts[ic];
+        V3 ma = v3(-dir.x, -dir.y, -dir.z), mb = Bv - A, mc = Cv - A;
+        V3 bc = cross(mb, mc), ca = cross(mc, ma), ab = cross(ma, mb);
+        double det = dot(ma, bc);
+        if (det == 0.0) continue;
+        double id = -1.0 / det;
+        V3 w = v3(id * (g_t * bc.x + g_al * ca.x + g_be * ab.x), id * (g_t * bc.y + g_al * ca.y + g_be * ab.y),
+                  id * (g_t * bc.z + g_al * ca.z + g_be * ab.z));
+        double wa = 1.0 - (hh.alpha + hh.beta), wb = hh.alpha, wc = hh.beta;
+        for (int c = 0; c < 3; c++) {
+          add(grad_v + 3 * ia + c, wa * comp(w, c));
+          add(grad_v + 3 * ib + c, wb * comp(w, c));
+          add(grad_v + 3 * ic + c, wc * comp(w, c));
+        }
+      }
+    }
+  }
 }
 
 int orc_num_threads() {

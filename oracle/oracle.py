@@ -142,21 +142,45 @@ class OracleScene:
         hid = np.zeros(npx * spp, np.int32) if aux else None
         ht = np.zeros(npx * spp, np.float64) if aux else None
         sh = np.zeros(npx * spp, np.int32) if aux else None
+        shid = np.zeros(npx * spp, np.int32) if aux else None
         ro = np.zeros((npx * spp, 6), np.float64) if rays_out else None
         ri = None if rays_in is None else np.ascontiguousarray(rays_in, np.float64)
         f = self.lib.orc_render
         f.restype = C.c_int
         f.argtypes = [C.c_void_p, C.POINTER(_Cam), C.POINTER(_Light), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
-                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                      C.c_void_p]
         g = lambda a: None if a is None else a.ctypes.data  # noqa: E731
         ov = f(self.h, C.byref(c), C.byref(L), width, height, spp, r0, r1, rgb.ctypes.data, col.ctypes.data,
-               g(hid), g(ht), g(sh), g(ri), g(ro), nthreads)
+               g(hid), g(ht), g(sh), g(ri), g(ro), nthreads, g(shid))
         out = dict(rgb=rgb, color=col, overflow=ov)
         if aux:
-            out.update(hit_id=hid, hit_t=ht, shadow=sh)
+            out.update(hit_id=hid, hit_t=ht, shadow=sh, shadow_id=shid)
         if rays_out:
             out["rays"] = ro
         return out
+
+
+def _adjoint(self, cam, light, width, height, spp, grad_rgb, grad_depth=None, nthreads=0):
+    """Float64 reference gradient (orc_adjoint)."""
+    assert self.kind == "oracle"
+    c = _Cam(cam.fov, cam.focal_point, cam.fstop, (C.c_double * 3)(*cam.eye))
+    L = _Light((C.c_double * 3)(*light.color), (C.c_double * 3)(*light.position), light.radius,
+               light.constant_term, light.linear_term, light.quadratic_term)
+    g = np.ascontiguousarray(grad_rgb, np.float64)
+    gd = None if grad_depth is None else np.ascontiguousarray(grad_depth, np.float64)
+    gv = np.zeros((self.mesh.verts.shape[0], 3))
+    gl = np.zeros(3)
+    gk = np.zeros((np.asarray(self.mesh.materials).reshape(-1, 16).shape[0], 3))
+    f = self.lib.orc_adjoint
+    f.argtypes = [C.c_void_p, C.POINTER(_Cam), C.POINTER(_Light), C.c_int, C.c_int, C.c_int, C.c_void_p,
+                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+    f(self.h, C.byref(c), C.byref(L), width, height, spp, g.ctypes.data, None if gd is None else gd.ctypes.data,
+      gv.ctypes.data, gl.ctypes.data, gk.ctypes.data, nthreads)
+    return dict(vertices=gv, light=gl, kd=gk)
+
+
+OracleScene.adjoint = _adjoint
 
 
 def ref_available() -> bool:
