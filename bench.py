@@ -206,6 +206,7 @@ def run_crt(args, dist, rank, ws):
     ok_img = bool(np.array_equal(rgb_h.numpy(), rgb.cpu().numpy()))
 
     refit = run_refit_vs_rebuild() if (rank == 0 and not args.no_extras) else None
+    batched = run_batched() if (rank == 0 and not args.no_extras) else None
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(sc, args.cpu_seconds)
@@ -235,6 +236,8 @@ def run_crt(args, dist, rank, ws):
     }
     if refit is not None:
         line["refit_vs_rebuild"] = refit
+    if batched is not None:
+        line["batched_vs_plain"] = batched
     if cpu is not None:
         line["cpu_baseline"] = cpu
     return line
@@ -280,6 +283,70 @@ def run_refit_vs_rebuild(frames=60, W2=1280, H2=720, spp=4):
             "refit_frame_ms": round(res["refit"][1], 3), "rebuild_frame_ms": round(res["rebuild"][1], 3),
             "refit_mrays_s": round(rays / res["refit"][1] / 1e3, 1),
             "rebuild_mrays_s": round(rays / res["rebuild"][1] / 1e3, 1)}
+
+
+def run_batched(count=256, reps=3):
+    """The batched workload: 256 meshes (log-uniform 1k..500k triangles),
+    each with its own camera and light, 256x256 at 4 spp.  Batched = one
+    graph replay of the segmented build + the persistent multi-scene render,
+    after the autotuner chose the launch shape; plain = the 256 meshes built
+    and rendered one after another with the plain entry points (scenes
+    resident on the device).  Both timed with CUDA events, L2 flushed first;
+    the images of both must be identical."""
+    import torch
+
+    import crt
+    from crt import data
+    scs = data.config3(count=count)
+    views = [(s.camera, s.light, s.width, s.height, s.spp) for s in scs]
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    b = crt.Batch([s.mesh for s in scs], views)
+    total_px = int(b.offsets[-1])
+    rays = b.rays
+    tris = sum(b.ntri)
+    img_b = torch.empty((total_px, 3), dtype=torch.uint8, device="cuda")
+    tune = b.autotune(stream=stream)
+    for _ in range(2):
+        b.run(img_b, graph=True, stream=stream)
+    torch.cuda.synchronize()
+    b.check()
+
+    def timed(fn):
+        ts = []
+        for _ in range(reps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    t_batch = timed(lambda: b.run(img_b, graph=True, stream=stream))
+    scenes = [crt.Scene(s.mesh) for s in scs]
+    img_p = torch.empty((total_px, 3), dtype=torch.uint8, device="cuda")
+    outs = [{"rgb8": img_p[b.offsets[m]:b.offsets[m + 1]]} for m in range(count)]
+
+    def plain():
+        for m, s in enumerate(scs):
+            scenes[m].build(stream=stream)
+            scenes[m].render(s.camera, s.light, s.width, s.height, s.spp, out=outs[m], stream=stream)
+
+    plain()
+    torch.cuda.synchronize()
+    t_plain = timed(plain)
+    same = bool(torch.equal(img_b, img_p))
+    for s in scenes:
+        s.check()
+        s.close()
+    b.close()
+    return {"meshes": count, "triangles": tris, "rays": rays, "image": "256x256x4spp per mesh",
+            "batched_ms": round(t_batch, 3), "plain_ms": round(t_plain, 3),
+            "batched_mrays_s": round(rays / t_batch / 1e3, 1), "plain_mrays_s": round(rays / t_plain / 1e3, 1),
+            "speedup": round(t_plain / t_batch, 3), "tuning": tune, "images_identical": same,
+            "plain_launches": 9 * count, "batched_launches": 12}
 
 
 def _cpu_impl():
@@ -358,7 +425,7 @@ def main():
     ap.add_argument("--impl", default="crt", choices=["crt", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-extras", action="store_true", help="skip the refit-vs-rebuild figures")
+    ap.add_argument("--no-extras", action="store_true", help="skip the refit-vs-rebuild and batched-vs-plain figures")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "crt" else args.warmup
     dist, rank, ws = dist_setup()

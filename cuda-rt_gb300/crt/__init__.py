@@ -20,7 +20,7 @@ import numpy as np
 from . import data  # noqa: F401
 from .build import LIB as LIB_PATH
 
-__all__ = ["CrtError", "Scene", "lib", "sort_pairs", "sort_pairs_noalloc", "morton", "STATUS", "render_args"]
+__all__ = ["CrtError", "Scene", "Batch", "lib", "sort_pairs", "sort_pairs_noalloc", "morton", "STATUS", "render_args"]
 
 STATUS = {0: "CRT_OK", 1: "CRT_INVALID_ARG", 2: "CRT_OOM", 3: "CRT_CUDA_ERROR", 4: "CRT_STACK_OVERFLOW",
           5: "CRT_TIMEOUT", 6: "CRT_NOT_BUILT"}
@@ -64,6 +64,16 @@ class _RenderOut(C.Structure):
                 ("rgb_f64", C.c_void_p), ("depth", C.c_void_p), ("shadow_id", C.c_void_p)]
 
 
+class _BatchView(C.Structure):
+    _fields_ = [("camera", _Camera), ("light", _Light), ("width", C.c_int32), ("height", C.c_int32),
+                ("spp", C.c_int32)]
+
+
+class _BatchTuning(C.Structure):
+    _fields_ = [("block_size", C.c_int32), ("tile_w", C.c_int32), ("tile_h", C.c_int32), ("stack", C.c_int32),
+                ("render_ms", C.c_float)]
+
+
 _lib = None
 
 
@@ -91,6 +101,13 @@ def lib():
             "crt_scene_check": [vp, vp],
             "crt_scene_set_materials": [vp, vp, i32, vp],
             "crt_adjoint_lambert": [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp],
+            "crt_batch_create": [vp, vp, i32, vp, vp],
+            "crt_batch_destroy": [vp],
+            "crt_batch_run": [vp, i32, vp, vp],
+            "crt_batch_set_tuning": [vp, vp],
+            "crt_batch_autotune": [vp, vp, vp],
+            "crt_batch_export": [vp, i32, vp, vp, vp, vp, vp, vp],
+            "crt_batch_check": [vp, vp],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -247,6 +264,87 @@ class Scene:
         o = _RenderOut(*[_addr(out.get(k)) for k in ("rgb8", "rgb_f32", "hit_id", "hit_t", "shadow", "rays",
                                                      "traversal_stats", "rgb_f64", "depth", "shadow_id")])
         _check(lib().crt_render(self.h, C.byref(cam), C.byref(lt), C.byref(p), C.byref(o), _stream(stream)))
+        return out
+
+
+class Batch:
+    """Many meshes, each with its own camera, light and image size, built and
+    rendered together (crt_batch_*).  `meshes` are data.Mesh objects, `views`
+    (camera, light, width, height, spp) tuples."""
+
+    def __init__(self, meshes, views, stream=None):
+        keep = []
+
+        def hold(a, dt):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dt)
+            keep.append(a)
+            return a.ctypes.data
+
+        M = len(meshes)
+        descs = (_MeshDesc * M)()
+        vws = (_BatchView * M)()
+        self.sizes, self.ntri = [], []
+        for m, (mesh, (cam, light, w, h, spp)) in enumerate(zip(meshes, views)):
+            mats = np.asarray(mesh.materials, np.float64).reshape(-1, 16)
+            descs[m] = _MeshDesc(hold(mesh.verts, np.float32), int(mesh.verts.shape[0]),
+                                 hold(mesh.normals, np.float32), int(mesh.normals.shape[0]),
+                                 hold(mesh.vidx, np.int32), hold(mesh.nidx, np.int32), int(mesh.vidx.shape[0]),
+                                 hold(mats, np.float64), int(mats.shape[0]), hold(mesh.matid, np.int32))
+            c, lt, _ = render_args(cam, light, w, h, spp)
+            vws[m] = _BatchView(c, lt, w, h, spp)
+            self.sizes.append((w, h, spp))
+            self.ntri.append(int(mesh.vidx.shape[0]))
+        self.M = M
+        self.pixels = [w * h for (w, h, _) in self.sizes]
+        self.offsets = np.concatenate([[0], np.cumsum(self.pixels)]).astype(np.int64)
+        self.rays = sum(w * h * s for (w, h, s) in self.sizes)
+        h = C.c_void_p()
+        _check(lib().crt_batch_create(descs, vws, M, _stream(stream), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().crt_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, out=None, graph=True, stream=None):
+        """Build and render everything; `out` is a (total pixels, 3) uint8
+        NumPy array or CUDA tensor, or None to keep the images on the device."""
+        _check(lib().crt_batch_run(self.h, int(bool(graph)), _addr(out), _stream(stream)))
+        return out
+
+    def images(self, out):
+        """Split run()'s concatenated output into per-mesh (W*H, 3) views."""
+        return [out[self.offsets[m]:self.offsets[m + 1]] for m in range(self.M)]
+
+    def set_tuning(self, block_size, tile_w, tile_h, stack):
+        t = _BatchTuning(block_size, tile_w, tile_h, stack, 0.0)
+        _check(lib().crt_batch_set_tuning(self.h, C.byref(t)))
+
+    def autotune(self, stream=None):
+        t = _BatchTuning()
+        _check(lib().crt_batch_autotune(self.h, C.byref(t), _stream(stream)))
+        return dict(block_size=t.block_size, tile_w=t.tile_w, tile_h=t.tile_h, stack=t.stack,
+                    render_ms=float(t.render_ms))
+
+    def check(self, stream=None):
+        _check(lib().crt_batch_check(self.h, _stream(stream)))
+
+    def export(self, m, stream=None) -> dict:
+        n = self.ntri[m]
+        nn = 2 * n - 1
+        out = dict(scene_box=np.zeros(6, np.float32), codes=np.zeros(n, np.int32), ids=np.zeros(n, np.uint32),
+                   nodes=np.zeros((nn, 3), np.int32), node_boxes=np.zeros((nn, 6), np.float32))
+        _check(lib().crt_batch_export(self.h, m, *[_addr(out[k]) for k in ("scene_box", "codes", "ids", "nodes",
+                                                                            "node_boxes")], _stream(stream)))
         return out
 
 

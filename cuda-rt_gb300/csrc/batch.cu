@@ -1,0 +1,432 @@
+// batch.cu -- the batched form: many meshes, each with its own camera and
+// light, built and rendered together.  The build runs as one sequence of
+// segmented kernels over all meshes (build.cu, "batched"); the render is one
+// persistent launch whose warps claim (mesh, pixel tile) work items.  The
+// whole sequence is captured once into a CUDA graph and replayed.  The block
+// size, the warp's pixel tile and the shared-memory part of the traversal
+// stack are chosen by crt_batch_autotune.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/crt.h"
+#include "crt_internal.h"
+
+namespace crt {
+void set_last_error(const char* msg);
+}
+
+using namespace crt;
+
+struct crt_batch {
+  int M = 0, N = 0, V = 0, Nn = 0, Mat = 0;
+  std::vector<int> tri_off, px_off;  // host copies
+  std::vector<int> item_off;           // kTileShapes x (M + 1): work-item prefix per tile shape
+  int* d_item_off = nullptr;
+  std::vector<crt_batch_view> views;
+  void* block = nullptr;  // one allocation for everything
+  BatchBufs b;
+  BatchView v;
+  uint8_t* image = nullptr;  // concatenated rgb8 images
+  size_t image_bytes = 0;
+  RenderArgs* args = nullptr;
+  BatchTuning tuning;
+  cudaStream_t cap = nullptr;  // capture stream (the legacy stream cannot be captured)
+  cudaGraphExec_t graph = nullptr;
+};
+
+namespace {
+
+crt_status fail(crt_status s, const std::string& m) {
+  crt::set_last_error(m.c_str());
+  return s;
+}
+crt_status cuda_fail(cudaError_t e, const char* what) {
+  cudaGetLastError();
+  return fail(e == cudaErrorMemoryAllocation ? CRT_OOM : CRT_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define CRT_CUDA(call, what)                               \
+  do {                                                     \
+    cudaError_t e_ = (call);                               \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what);     \
+  } while (0)
+
+size_t al(size_t x) { return (x + 255) & ~size_t(255); }
+
+bool on_device(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+constexpr int kTileShapes = 4;
+constexpr int kTileW[kTileShapes] = {8, 4, 16, 32};
+
+int shape_of(const BatchTuning& t) {
+  for (int s = 0; s < kTileShapes; s++)
+    if (kTileW[s] == t.tw) return s;
+  return 0;
+}
+
+// The device view for tuning t (the work-item prefix depends on the tile shape).
+BatchView view_for(const crt_batch* b, const BatchTuning& t) {
+  BatchView v = b->v;
+  const int s = shape_of(t);
+  v.item_off = b->d_item_off + (size_t)s * (b->M + 1);
+  v.items = b->item_off[(size_t)s * (b->M + 1) + b->M];
+  return v;
+}
+
+cudaError_t enqueue(crt_batch* b, cudaStream_t st) {
+  cudaError_t e = launch_build_batch(b->b, st);
+  if (e != cudaSuccess) return e;
+  return launch_render_batch(view_for(b, b->tuning), b->tuning, st);
+}
+
+void drop_graph(crt_batch* b) {
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* views, int32_t M, void* stream,
+                            crt_batch** out) {
+  if (!meshes || !views || !out || M <= 0) return fail(CRT_INVALID_ARG, "bad arguments");
+  *out = nullptr;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  crt_batch* b = new crt_batch;
+  b->M = M;
+  b->tri_off.assign(M + 1, 0);
+  if (M > kRadix) {
+    delete b;
+    return fail(CRT_INVALID_ARG, "at most " + std::to_string(kRadix) + " meshes in a batch");
+  }
+  b->item_off.assign((size_t)kTileShapes * (M + 1), 0);
+  b->px_off.assign(M + 1, 0);
+  std::vector<int> vert_off(M + 1, 0), nrm_off(M + 1, 0), mat_off(M + 1, 0);
+  for (int m = 0; m < M; m++) {
+    const crt_mesh_desc& d = meshes[m];
+    const crt_batch_view& w = views[m];
+    if (d.num_triangles <= 0 || !d.vertices || !d.vertex_indices || !d.normals || !d.materials ||
+        d.num_materials <= 0 || w.width <= 0 || w.height <= 0 || w.spp <= 0) {
+      delete b;
+      return fail(CRT_INVALID_ARG, "batch mesh " + std::to_string(m) + ": bad description");
+    }
+    if (on_device(d.vertices) || on_device(d.vertex_indices)) {
+      delete b;
+      return fail(CRT_INVALID_ARG, "crt_batch_create takes host meshes");
+    }
+    for (int64_t i = 0; i < 3 * (int64_t)d.num_triangles; i++) {
+      const int32_t* ni = d.normal_indices ? d.normal_indices : d.vertex_indices;
+      if (d.vertex_indices[i] < 0 || d.vertex_indices[i] >= d.num_vertices || ni[i] < 0 || ni[i] >= d.num_normals) {
+        delete b;
+        return fail(CRT_INVALID_ARG, "batch mesh " + std::to_string(m) + ": index out of range");
+      }
+    }
+    for (int t = 0; d.material_ids && t < d.num_triangles; t++)
+      if (d.material_ids[t] < 0 || d.material_ids[t] >= d.num_materials) {
+        delete b;
+        return fail(CRT_INVALID_ARG, "batch mesh " + std::to_string(m) + ": material id out of range");
+      }
+    b->tri_off[m + 1] = b->tri_off[m] + d.num_triangles;
+    vert_off[m + 1] = vert_off[m] + d.num_vertices;
+    nrm_off[m + 1] = nrm_off[m] + d.num_normals;
+    mat_off[m + 1] = mat_off[m] + d.num_materials;
+    for (int sh = 0; sh < kTileShapes; sh++) {  // warp tiles of 32 pixels
+      const int tw = kTileW[sh], th = 32 / tw;
+      int* io = &b->item_off[(size_t)sh * (M + 1)];
+      io[m + 1] = io[m] + ((w.width + tw - 1) / tw) * ((w.height + th - 1) / th);
+    }
+    b->px_off[m + 1] = b->px_off[m] + w.width * w.height;
+    b->views.push_back(w);
+  }
+  const int N = b->tri_off[M], V = vert_off[M], Nn = nrm_off[M], Mat = mat_off[M];
+  if ((int64_t)N > CRT_MAX_TRIANGLES) {
+    delete b;
+    return fail(CRT_INVALID_ARG, "too many triangles in the batch");
+  }
+  b->N = N, b->V = V, b->Nn = Nn, b->Mat = Mat;
+  // host staging of the concatenated arrays (indices made global)
+  std::vector<float> hv(3 * (size_t)V), hn(3 * (size_t)Nn);
+  std::vector<int> hvi(3 * (size_t)N), hni(3 * (size_t)N), hmat(N), hmesh(N);
+  std::vector<crt_material> hm(Mat);
+  for (int m = 0; m < M; m++) {
+    const crt_mesh_desc& d = meshes[m];
+    std::memcpy(&hv[3 * (size_t)vert_off[m]], d.vertices, 12 * (size_t)d.num_vertices);
+    std::memcpy(&hn[3 * (size_t)nrm_off[m]], d.normals, 12 * (size_t)d.num_normals);
+    std::memcpy(&hm[mat_off[m]], d.materials, sizeof(crt_material) * d.num_materials);
+    const int32_t* ni = d.normal_indices ? d.normal_indices : d.vertex_indices;
+    for (int t = 0; t < d.num_triangles; t++) {
+      const size_t g = (size_t)b->tri_off[m] + t;
+      for (int k = 0; k < 3; k++) {
+        hvi[3 * g + k] = vert_off[m] + d.vertex_indices[3 * t + k];
+        hni[3 * g + k] = nrm_off[m] + ni[3 * t + k];
+      }
+      hmat[g] = mat_off[m] + (d.material_ids ? d.material_ids[t] : 0);
+      hmesh[g] = m;
+    }
+  }
+  // one device block
+  const int tiles = sort_tiles(N);
+  const int NI = N - M;
+  b->image_bytes = 3 * (size_t)b->px_off[M];
+  const size_t sz[] = {12 * (size_t)V, 12 * (size_t)Nn, 12 * (size_t)N, 12 * (size_t)N, 4 * (size_t)N,
+                       sizeof(DMat) * (size_t)Mat, 4 * (size_t)N, 4 * (size_t)(M + 1), 4 * (size_t)kTileShapes * (M + 1),
+                       5 * 4 * (size_t)N, 4 * 4 * (size_t)kRadix, 4 * 4 * (size_t)tiles * kRadix,
+                       4 * (size_t)(NI + N), 4 * (size_t)(NI > 0 ? NI : 1), sizeof(BNode) * (size_t)(NI > 0 ? NI : 1),
+                       sizeof(LeafTri) * (size_t)N, sizeof(SceneGlobals) * (size_t)M, 64, b->image_bytes,
+                       sizeof(RenderArgs) * (size_t)M};
+  const int K = sizeof(sz) / sizeof(sz[0]);
+  std::vector<size_t> off(K);
+  size_t total = 0;
+  for (int i = 0; i < K; i++) off[i] = total, total += al(sz[i]);
+  cudaError_t e = cudaMalloc(&b->block, total);
+  if (e != cudaSuccess) {
+    delete b;
+    return cuda_fail(e, "cudaMalloc");
+  }
+  char* base = static_cast<char*>(b->block);
+  auto at = [&](int i) { return base + off[i]; };
+  float* d_v = (float*)at(0);
+  float* d_n = (float*)at(1);
+  int* d_vi = (int*)at(2);
+  int* d_ni = (int*)at(3);
+  int* d_mat = (int*)at(4);
+  DMat* d_mats = (DMat*)at(5);
+  int* d_mesh = (int*)at(6);
+  int* d_toff = (int*)at(7);
+  int* d_ioff = (int*)at(8);
+  uint32_t* keys = (uint32_t*)at(9);
+  BatchBufs& bb = b->b;
+  bb.M = M, bb.N = N, bb.NI = NI;
+  bb.verts = d_v, bb.vidx = d_vi, bb.mesh_of = d_mesh, bb.tri_off = d_toff;
+  bb.keys_a = keys, bb.keys_b = keys + N, bb.vals_a = keys + 2 * (size_t)N, bb.vals_b = keys + 3 * (size_t)N;
+  bb.codes0 = keys + 4 * (size_t)N;
+  bb.hist = (uint32_t*)at(10);
+  bb.status = (uint32_t*)at(11);
+  bb.parent = (uint32_t*)at(12);
+  bb.flags = (int*)at(13);
+  bb.nodes = (BNode*)at(14);
+  bb.leaves = (LeafTri*)at(15);
+  bb.g = (SceneGlobals*)at(16);
+  bb.counters = (unsigned*)at(17);
+  bb.err = (int*)(at(17) + 32);
+  b->image = (uint8_t*)at(18);
+  b->args = (RenderArgs*)at(19);
+  BatchView& v = b->v;
+  b->d_item_off = d_ioff;
+  v.M = M, v.tri_off = d_toff;
+  v.verts = d_v, v.normals = d_n, v.vidx = d_vi, v.nidx = d_ni, v.matid = d_mat, v.mats = d_mats;
+  v.nodes = bb.nodes, v.leaves = bb.leaves, v.g = bb.g, v.args = b->args;
+  v.counter = bb.counters + 4;
+  // per-mesh render arguments
+  std::vector<RenderArgs> ha(M);
+  for (int m = 0; m < M; m++) {
+    const crt_batch_view& w = views[m];
+    RenderArgs& a = ha[m];
+    std::memset(&a, 0, sizeof(a));
+    a.W = w.width, a.H = w.height, a.spp = w.spp, a.row0 = 0, a.row1 = w.height;
+    a.angle = std::tan(M_PI * 0.5 * w.camera.fov / 180.0f);
+    a.aspect = double(w.width) / double(w.height);
+    a.invW = 1.0 / double(w.width);
+    a.invH = 1.0 / double(w.height);
+    a.aperture = 1 / w.camera.fstop;
+    a.focal = w.camera.focal_point;
+    for (int k = 0; k < 3; k++) {
+      a.eye[k] = w.camera.eye[k];
+      a.lpos[k] = w.light.position[k];
+      a.lcol[k] = w.light.color[k];
+    }
+    a.lradius = w.light.radius;
+    a.latt[0] = w.light.constant_term, a.latt[1] = w.light.linear_term, a.latt[2] = w.light.quadratic_term;
+    a.rgb8 = b->image + 3 * (size_t)b->px_off[m];
+  }
+  static_assert(sizeof(DMat) == sizeof(crt_material), "material layout");
+  auto up = [&](void* dst, const void* src, size_t n) {
+    return n ? cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, st) : cudaSuccess;
+  };
+  if ((e = up(d_v, hv.data(), 4 * hv.size())) != cudaSuccess || (e = up(d_n, hn.data(), 4 * hn.size())) != cudaSuccess ||
+      (e = up(d_vi, hvi.data(), 4 * hvi.size())) != cudaSuccess ||
+      (e = up(d_ni, hni.data(), 4 * hni.size())) != cudaSuccess ||
+      (e = up(d_mat, hmat.data(), 4 * hmat.size())) != cudaSuccess ||
+      (e = up(d_mats, hm.data(), sizeof(crt_material) * hm.size())) != cudaSuccess ||
+      (e = up(d_mesh, hmesh.data(), 4 * hmesh.size())) != cudaSuccess ||
+      (e = up(d_toff, b->tri_off.data(), 4 * (M + 1))) != cudaSuccess ||
+      (e = up(d_ioff, b->item_off.data(), 4 * b->item_off.size())) != cudaSuccess ||
+      (e = up(b->args, ha.data(), sizeof(RenderArgs) * M)) != cudaSuccess ||
+      (e = cudaMemsetAsync(bb.flags, 0, sz[13], st)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(st)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking)) != cudaSuccess) {
+    cudaFree(b->block);
+    delete b;
+    return cuda_fail(e, "batch upload");
+  }
+  *out = b;
+  return CRT_OK;
+}
+
+crt_status crt_batch_destroy(crt_batch* b) {
+  if (!b) return CRT_OK;
+  cudaDeviceSynchronize();
+  drop_graph(b);
+  if (b->cap) cudaStreamDestroy(b->cap);
+  cudaFree(b->block);
+  delete b;
+  return CRT_OK;
+}
+
+crt_status crt_batch_set_tuning(crt_batch* b, const crt_batch_tuning* t) {
+  if (!b || !t) return fail(CRT_INVALID_ARG, "null argument");
+  const bool ok = (t->block_size == 64 || t->block_size == 128 || t->block_size == 256) && t->tile_w > 0 &&
+                  t->tile_h > 0 && t->tile_w * t->tile_h == 32 && (t->stack == 0 || t->stack == 8 || t->stack == 16);
+  if (!ok) return fail(CRT_INVALID_ARG, "unsupported tuning");
+  b->tuning.block = t->block_size, b->tuning.tw = t->tile_w, b->tuning.th = t->tile_h, b->tuning.stack = t->stack;
+  drop_graph(b);
+  return CRT_OK;
+}
+
+crt_status crt_batch_run(crt_batch* b, int use_graph, uint8_t* rgb8, void* stream) {
+  if (!b) return fail(CRT_INVALID_ARG, "null batch");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (use_graph) {
+    if (!b->graph) {
+      cudaGraph_t g = nullptr;
+      CRT_CUDA(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal), "begin capture");
+      cudaError_t e = enqueue(b, b->cap);
+      cudaError_t e2 = cudaStreamEndCapture(b->cap, &g);
+      if (e != cudaSuccess) return cuda_fail(e, "capture");
+      if (e2 != cudaSuccess) return cuda_fail(e2, "end capture");
+      e = cudaGraphInstantiate(&b->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return cuda_fail(e, "instantiate");
+    }
+    CRT_CUDA(cudaGraphLaunch(b->graph, st), "graph launch");
+  } else {
+    CRT_CUDA(enqueue(b, st), "batch launch");
+  }
+  if (rgb8) CRT_CUDA(cudaMemcpyAsync(rgb8, b->image, b->image_bytes, cudaMemcpyDefault, st), "download");
+  if (rgb8 && !on_device(rgb8)) CRT_CUDA(cudaStreamSynchronize(st), "synchronize");
+  return CRT_OK;
+}
+
+crt_status crt_batch_check(crt_batch* b, void* stream) {
+  if (!b) return fail(CRT_INVALID_ARG, "null batch");
+  CRT_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)), "synchronize");
+  int err = 0;
+  CRT_CUDA(cudaMemcpy(&err, b->b.err, sizeof(int), cudaMemcpyDeviceToHost), "read");
+  std::vector<SceneGlobals> g(b->M);
+  CRT_CUDA(cudaMemcpy(g.data(), b->b.g, sizeof(SceneGlobals) * b->M, cudaMemcpyDeviceToHost), "read");
+  for (auto& x : g) err |= x.err;
+  if (err & kErrTimeout) return fail(CRT_TIMEOUT, "a radix-sort look-back wait timed out");
+  if (err & kErrStack) return fail(CRT_STACK_OVERFLOW, "a traversal exceeded the 64-entry stack");
+  if (err & kErrNonFinite) return fail(CRT_INVALID_ARG, "non-finite (or |x| > 1e37) vertex coordinate");
+  return CRT_OK;
+}
+
+// Times every supported tuning on the batch (build + render each, the graph
+// not used) and keeps the fastest; fills `chosen` if given.
+crt_status crt_batch_autotune(crt_batch* b, crt_batch_tuning* chosen, void* stream) {
+  if (!b) return fail(CRT_INVALID_ARG, "null batch");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int blocks[] = {64, 128, 256};
+  const int tiles[][2] = {{8, 4}, {4, 8}, {16, 2}, {32, 1}};
+  const int stacks[] = {0, 8, 16};
+  cudaEvent_t e0, e1;
+  CRT_CUDA(cudaEventCreate(&e0), "event");
+  CRT_CUDA(cudaEventCreate(&e1), "event");
+  BatchTuning best = b->tuning;
+  float best_ms = 1e30f;
+  CRT_CUDA(launch_build_batch(b->b, st), "build");
+  for (int bs : blocks)
+    for (auto& tl : tiles)
+      for (int sk : stacks) {
+        BatchTuning t;
+        t.block = bs, t.tw = tl[0], t.th = tl[1], t.stack = sk;
+        const BatchView v = view_for(b, t);
+        CRT_CUDA(launch_render_batch(v, t, st), "render");  // warm-up
+        CRT_CUDA(cudaEventRecord(e0, st), "event");
+        CRT_CUDA(launch_render_batch(v, t, st), "render");
+        CRT_CUDA(cudaEventRecord(e1, st), "event");
+        CRT_CUDA(cudaEventSynchronize(e1), "event");
+        float ms = 0.f;
+        CRT_CUDA(cudaEventElapsedTime(&ms, e0, e1), "event");
+        if (ms < best_ms) best_ms = ms, best = t;
+      }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->tuning = best;
+  drop_graph(b);
+  if (chosen) {
+    chosen->block_size = best.block, chosen->tile_w = best.tw, chosen->tile_h = best.th, chosen->stack = best.stack;
+    chosen->render_ms = best_ms;
+  }
+  return CRT_OK;
+}
+
+// The build products of one mesh of the batch, in crt_bvh_export's layout.
+crt_status crt_batch_export(crt_batch* b, int32_t m, float* scene_box, int32_t* codes, uint32_t* ids,
+                            int32_t* nodes3, float* node_boxes, void* stream) {
+  if (!b || m < 0 || m >= b->M) return fail(CRT_INVALID_ARG, "bad mesh index");
+  CRT_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)), "synchronize");
+  const int t0 = b->tri_off[m], n = b->tri_off[m + 1] - t0, NI = b->b.NI, ib = t0 - m;
+  const size_t nn = 2 * (size_t)n - 1;
+  SceneGlobals g;
+  CRT_CUDA(cudaMemcpy(&g, b->b.g + m, sizeof(g), cudaMemcpyDeviceToHost), "download");
+  auto ord2f_h = [](int i) {
+    int bits = i >= 0 ? i : i ^ 0x7FFFFFFF;
+    float f;
+    std::memcpy(&f, &bits, 4);
+    return f;
+  };
+  std::vector<uint32_t> hk(n), hv(n), par_i(n > 1 ? n - 1 : 0), par_l(n);
+  std::vector<BNode> nd(n > 1 ? n - 1 : 0);
+  CRT_CUDA(cudaMemcpy(hk.data(), b->b.keys_b + t0, 4 * (size_t)n, cudaMemcpyDeviceToHost), "download");
+  CRT_CUDA(cudaMemcpy(hv.data(), b->b.vals_a + t0, 4 * (size_t)n, cudaMemcpyDeviceToHost), "download");
+  CRT_CUDA(cudaMemcpy(par_l.data(), b->b.parent + NI + t0, 4 * (size_t)n, cudaMemcpyDeviceToHost), "download");
+  if (n > 1) {
+    CRT_CUDA(cudaMemcpy(par_i.data(), b->b.parent + ib, 4 * (size_t)(n - 1), cudaMemcpyDeviceToHost), "download");
+    CRT_CUDA(cudaMemcpy(nd.data(), b->b.nodes + ib, sizeof(BNode) * (n - 1), cudaMemcpyDeviceToHost), "download");
+  }
+  const uint32_t mask = (1u << 30) - 1;
+  std::vector<int> n3(3 * nn);
+  std::vector<float> nb(6 * nn);
+  auto ref = [n](int code) { return code >= 0 ? code : (n - 1) + ~code; };
+  for (int i = 0; i < n - 1; i++) n3[3 * i] = i == 0 ? -1 : (int)(par_i[i] & mask) - ib;
+  for (int k = 0; k < n; k++) {
+    n3[3 * ((n - 1) + k)] = n > 1 ? (int)(par_l[k] & mask) - ib : -1;
+    n3[3 * ((n - 1) + k) + 1] = n3[3 * ((n - 1) + k) + 2] = (int)hv[k] - t0;
+  }
+  for (int i = 0; i < n - 1; i++) {
+    const BNode& q = nd[i];
+    const int l = ref(q.child.x), r = ref(q.child.y);
+    n3[3 * i + 1] = l, n3[3 * i + 2] = r;
+    const float lb[6] = {q.xy_l.x, q.xy_l.z, q.z_lr.x, q.xy_l.y, q.xy_l.w, q.z_lr.y};
+    const float rbx[6] = {q.xy_r.x, q.xy_r.z, q.z_lr.z, q.xy_r.y, q.xy_r.w, q.z_lr.w};
+    std::memcpy(&nb[6 * (size_t)l], lb, sizeof(lb));
+    std::memcpy(&nb[6 * (size_t)r], rbx, sizeof(rbx));
+  }
+  std::memcpy(&nb[0], g.root_box, 6 * sizeof(float));
+  float box[6];
+  for (int k = 0; k < 3; k++) box[k] = ord2f_h(g.bmin[k]), box[3 + k] = ord2f_h(g.bmax[k]);
+  std::vector<int32_t> ids_local(n);
+  for (int k = 0; k < n; k++) ids_local[k] = (int32_t)hv[k] - t0;
+  auto put = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+    return (dst && bytes) ? cudaMemcpy(dst, src, bytes, cudaMemcpyDefault) : cudaSuccess;
+  };
+  CRT_CUDA(put(scene_box, box, sizeof(box)), "export");
+  CRT_CUDA(put(codes, hk.data(), 4 * (size_t)n), "export");
+  CRT_CUDA(put(ids, ids_local.data(), 4 * (size_t)n), "export");
+  CRT_CUDA(put(nodes3, n3.data(), 4 * n3.size()), "export");
+  CRT_CUDA(put(node_boxes, nb.data(), 4 * nb.size()), "export");
+  return CRT_OK;
+}
+
+}  // extern "C"

@@ -621,6 +621,247 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__
   }
 }
 
+// ---------------------------------------------------------------- batched
+// The same build for many meshes at once (concatenated arrays; mesh m owns
+// triangles [tri_off[m], tri_off[m+1]) and internal nodes [int_off[m],
+// int_off[m+1]), int_off[m] = tri_off[m] - m).  Child codes in BNode are
+// local to the mesh, so each mesh's node and leaf ranges are a self-contained
+// tree for the traversal; parent words hold global internal indices.
+
+__global__ void k_batch_init(SceneGlobals* g, int M, uint32_t* hist, const int* __restrict__ tri_off,
+                             unsigned* counters, int* err) {
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) g[m].bmin[k] = f2ord(1e9f), g[m].bmax[k] = f2ord(-1e9f);
+    g[m].emax = f2ord(0.f);
+    g[m].err = 0;
+  }
+  // passes 0-2: code digits (filled by k_morton_batch); pass 3: the mesh id,
+  // whose histogram is the mesh sizes
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * kRadix; i += gridDim.x * blockDim.x) {
+    const int p = i / kRadix, d = i % kRadix;
+    hist[i] = (p == 3 && d < M) ? (uint32_t)(tri_off[d + 1] - tri_off[d]) : 0u;
+  }
+  if (blockIdx.x == 0 && threadIdx.x < 4) counters[threadIdx.x] = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *err = 0;
+}
+
+// Per-mesh scene bounds and largest triangle extent; warps whose lanes share
+// a mesh (nearly all) reduce before their atomics.
+__global__ void __launch_bounds__(256) k_bounds_batch(const float* __restrict__ V, const int* __restrict__ vidx,
+                                                      const int* __restrict__ mesh_of, int N, SceneGlobals* g) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int t0 = blockIdx.x * blockDim.x; t0 < N; t0 += stride) {
+    const int t = t0 + threadIdx.x;
+    float lo[3] = {1e9f, 1e9f, 1e9f}, hi[3] = {-1e9f, -1e9f, -1e9f}, e = 0.f;
+    bool ok = true;
+    int m = -1;
+    if (t < N) {
+      float3 a, b, c;
+      tri_box(V, vidx, t, a, b, c, lo, hi);
+      ok = finite_coords(a, b, c);
+      e = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+      m = __ldg(mesh_of + t);
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, m);
+    if (peers == 0xffffffffu) {  // one mesh in the whole warp
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+          hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+        }
+        e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, o));
+      }
+      ok = __all_sync(0xffffffffu, ok);
+      if ((threadIdx.x & 31) != 0) m = -1;
+    }
+    if (m >= 0) {
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        atomicMin(&g[m].bmin[k], f2ord(lo[k]));
+        atomicMax(&g[m].bmax[k], f2ord(hi[k]));
+      }
+      atomicMax(&g[m].emax, f2ord(e));
+      if (!ok) atomicOr(&g[m].err, kErrNonFinite);
+    }
+  }
+}
+
+// Morton codes against each triangle's own mesh box, a copy of the codes,
+// the digit histograms of the three code passes; clears the look-back status.
+__global__ void __launch_bounds__(512) k_morton_batch(const float* __restrict__ V, const int* __restrict__ vidx,
+                                                      const int* __restrict__ mesh_of, int N,
+                                                      const SceneGlobals* __restrict__ g, uint32_t* __restrict__ keys,
+                                                      uint32_t* __restrict__ codes0, uint32_t* __restrict__ hist,
+                                                      uint32_t* __restrict__ status, int status_words) {
+  __shared__ uint32_t sh[3 * kRadix];
+  for (int i = threadIdx.x; i < 3 * kRadix; i += blockDim.x) sh[i] = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < status_words; i += gridDim.x * blockDim.x) status[i] = 0;
+  __syncthreads();
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x) {
+    float3 a, b, c;
+    float lo[3], hi[3], mn[3], mx[3];
+    tri_box(V, vidx, t, a, b, c, lo, hi);
+    load_scene_box(g + __ldg(mesh_of + t), mn, mx);
+    const uint32_t code = morton_code(lo, hi, mn, mx);
+    keys[t] = code;
+    codes0[t] = code;
+    for (int p = 0; p < 3; p++) atomicAdd(&sh[p * kRadix + ((code >> (p * kRadixBits)) & (kRadix - 1))], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 3 * kRadix; i += blockDim.x)
+    if (sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+
+__global__ void k_mesh_keys(const uint32_t* __restrict__ vals, const int* __restrict__ mesh_of, int N,
+                            uint32_t* __restrict__ out) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < N; j += gridDim.x * blockDim.x)
+    out[j] = (uint32_t)__ldg(mesh_of + __ldg(vals + j));
+}
+
+__global__ void k_gather_codes(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ codes0, int N,
+                               uint32_t* __restrict__ out) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < N; j += gridDim.x * blockDim.x)
+    out[j] = __ldg(codes0 + __ldg(vals + j));
+}
+
+__device__ __forceinline__ int mesh_of_internal(const int* __restrict__ tri_off, int M, int gi) {
+  // last m with int_off[m] = tri_off[m] - m <= gi
+  int lo = 0, hi = M - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(tri_off + mid) - mid <= gi)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// BuildHierarchy per mesh (FindSpan/FindSplit on the mesh's sorted codes).
+__global__ void __launch_bounds__(256) k_hierarchy_batch(const uint32_t* __restrict__ codes_all,
+                                                         const int* __restrict__ tri_off, int M, int NI,
+                                                         BNode* __restrict__ nodes, uint32_t* __restrict__ parent,
+                                                         int* __restrict__ flags) {
+  const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= NI) return;
+  int m = mesh_of_internal(tri_off, M, gi);
+  // meshes with one triangle own no internal node: skip to the owner
+  while (m + 1 < M && __ldg(tri_off + m + 1) - (m + 1) <= gi) m++;
+  const int t0 = __ldg(tri_off + m);
+  const int n = __ldg(tri_off + m + 1) - t0;
+  const int i = gi - (t0 - m);
+  const uint32_t* codes = codes_all + t0;
+  const uint64_t ki = ((uint64_t)__ldg(codes + i) << 32) | (uint32_t)i;
+  const int dd = kdelta(codes, n, ki, i + 1) - kdelta(codes, n, ki, i - 1);
+  const int d = dd > 0 ? 1 : (dd < 0 ? -1 : 0);
+  const int dmin = kdelta(codes, n, ki, i - d);
+  int lmax = 2;
+  while (kdelta(codes, n, ki, i + lmax * d) > dmin) lmax *= 2;
+  int l = 0, t = lmax;
+  do {
+    t /= 2;
+    if (kdelta(codes, n, ki, i + (l + t) * d) > dmin) l += t;
+  } while (t > 1);
+  const int lo = min(i, i + l * d), hi = max(i, i + l * d);
+  int left = lo, right = hi;
+  uint64_t kl = ((uint64_t)__ldg(codes + left) << 32) | (uint32_t)left;
+  const int same = kdelta(codes, n, kl, right);
+  do {
+    const int s = (right + left) / 2;
+    if (kdelta(codes, n, kl, s) > same) {
+      left = s;
+      kl = ((uint64_t)__ldg(codes + left) << 32) | (uint32_t)left;
+    } else {
+      right = s;
+    }
+  } while (right > left + 1);
+  const int split = left;
+  const int c1 = (split == lo) ? ~split : split;
+  const int c2 = (split + 1 == hi) ? ~(split + 1) : split + 1;
+  nodes[gi].child = make_int4(c1, c2, 0, 0);
+  const int ib = t0 - m;  // this mesh's first internal node
+  const uint32_t spans = ((t0 + lo) / kRefitBlock != (t0 + hi) / kRefitBlock) ? kParentSpans : 0u;
+  parent[c1 < 0 ? NI + t0 + split : ib + split] = (uint32_t)gi | kParentLeft | spans;
+  parent[c2 < 0 ? NI + t0 + split + 1 : ib + split + 1] = (uint32_t)gi | spans;
+  flags[gi] = 0;
+}
+
+// RefitBounds per mesh; leaves at global sorted positions, the block-local /
+// spanning split as in k_refit (a node's shared slot is its first leaf's
+// global position).
+__global__ void __launch_bounds__(kRefitBlock) k_refit_batch(const float* __restrict__ V, const int* __restrict__ vidx,
+                                                             const uint32_t* __restrict__ ids,
+                                                             const int* __restrict__ mesh_of,
+                                                             const int* __restrict__ tri_off, int N, int NI,
+                                                             BNode* nodes, LeafTri* __restrict__ leaves,
+                                                             const uint32_t* __restrict__ parent, int* flags,
+                                                             SceneGlobals* g) {
+  __shared__ float s_box[kRefitBlock][2][6];
+  __shared__ int s_flag[kRefitBlock];
+  s_flag[threadIdx.x] = 0;
+  __syncthreads();
+  const int k0 = blockIdx.x * kRefitBlock;
+  const int k = k0 + threadIdx.x;
+  if (k >= N) return;
+  const int tri = (int)__ldg(ids + k);
+  const int m = __ldg(mesh_of + tri);
+  const int t0 = __ldg(tri_off + m);
+  const int n = __ldg(tri_off + m + 1) - t0;
+  float3 a, b, c;
+  float lo[3], hi[3];
+  tri_box(V, vidx, tri, a, b, c, lo, hi);
+  LeafTri lt;
+  lt.v0 = make_float4(a.x, a.y, a.z, __int_as_float(tri));
+  lt.v1 = make_float4(b.x, b.y, b.z, 0.f);
+  lt.v2 = make_float4(c.x, c.y, c.z, 0.f);
+  leaves[k] = lt;
+  if (n == 1) {
+#pragma unroll
+    for (int q = 0; q < 3; q++) g[m].root_box[q] = lo[q], g[m].root_box[3 + q] = hi[q];
+    return;
+  }
+  const int root = t0 - m;
+  uint32_t w = __ldg(parent + NI + k);
+  for (int level = 0;; level++) {
+    const int p = (int)(w & kParentMask);
+    if (level >= kStackSize || p < root || p >= root + n - 1) {  // only a corrupt tree gets here
+      atomicOr(&g[m].err, kErrStack);
+      return;
+    }
+    const uint32_t wn = (p == root) ? 0u : __ldg(parent + p);
+    BNode* P = nodes + p;
+    const bool is_left = (w & kParentLeft) != 0;
+    put_slot(P, is_left, lo, hi);
+    if (!(w & kParentSpans)) {
+      const int sl = p + m - k0;  // global leaf position of the node's index, within this block
+      float* mine = s_box[sl][is_left ? 0 : 1];
+#pragma unroll
+      for (int q = 0; q < 3; q++) mine[q] = lo[q], mine[3 + q] = hi[q];
+      __threadfence_block();
+      if (atomicAdd(&s_flag[sl], 1) == 0) return;
+      __threadfence_block();
+      const volatile float* o = s_box[sl][is_left ? 1 : 0];
+#pragma unroll
+      for (int q = 0; q < 3; q++) lo[q] = fminf(lo[q], o[q]), hi[q] = fmaxf(hi[q], o[3 + q]);
+    } else {
+      if ((atomic_add_acq_rel(flags + p, 1) & 1) == 0) return;
+      const float4 xl = __ldcg(&P->xy_l), xr = __ldcg(&P->xy_r), zz = __ldcg(&P->z_lr);
+      lo[0] = fminf(xl.x, xr.x), hi[0] = fmaxf(xl.y, xr.y);
+      lo[1] = fminf(xl.z, xr.z), hi[1] = fmaxf(xl.w, xr.w);
+      lo[2] = fminf(zz.x, zz.z), hi[2] = fmaxf(zz.y, zz.w);
+    }
+    if (p == root) {
+#pragma unroll
+      for (int q = 0; q < 3; q++) g[m].root_box[q] = lo[q], g[m].root_box[3 + q] = hi[q];
+      return;
+    }
+    w = wn;
+  }
+}
+
 }  // namespace
 
 namespace {
@@ -671,6 +912,41 @@ cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st)
   }
   if (n >= 2) k_hierarchy<<<(n - 1 + 255) / 256, 256, 0, st>>>(b.keys_b, n, b.nodes, b.parent, b.flags);
   refit(m, b, st);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_build_batch(const BatchBufs& b, cudaStream_t st) {
+  const int N = b.N, M = b.M;
+  if (N <= 0) return cudaSuccess;
+  const int tiles = sort_tiles(N);
+  const int sms = num_sms();
+  k_batch_init<<<(M + 255) / 256 > 4 ? (M + 255) / 256 : 4, 256, 0, st>>>(b.g, M, b.hist, b.tri_off, b.counters,
+                                                                         b.err);
+  k_bounds_batch<<<min((N + 255) / 256, sms * 8), 256, 0, st>>>(b.verts, b.vidx, b.mesh_of, N, b.g);
+  k_morton_batch<<<min((N + 511) / 512, sms * 2), 512, 0, st>>>(b.verts, b.vidx, b.mesh_of, N, b.g, b.keys_a,
+                                                                 b.codes0, b.hist, b.status,
+                                                                 4 * tiles * kRadix);
+  // code passes: a -> b -> a -> b
+  const uint32_t* kin = b.keys_a;
+  const uint32_t* vin = nullptr;
+  for (int p = 0; p < 3; p++) {
+    uint32_t* ko = (p & 1) ? b.keys_a : b.keys_b;
+    uint32_t* vo = (p & 1) ? b.vals_a : b.vals_b;
+    k_onesweep<<<tiles, kSortThreads, 0, st>>>(kin, vin, ko, vo, N, p * kRadixBits, b.hist + p * kRadix,
+                                                b.status + (size_t)p * tiles * kRadix, b.counters + p, b.err);
+    kin = ko;
+    vin = vo;
+  }
+  // stable pass on the mesh id: ids end up grouped by mesh, by code within
+  const int ge = min((N + 255) / 256, sms * 8);
+  k_mesh_keys<<<ge, 256, 0, st>>>(b.vals_b, b.mesh_of, N, b.keys_a);
+  k_onesweep<<<tiles, kSortThreads, 0, st>>>(b.keys_a, b.vals_b, b.keys_b, b.vals_a, N, 0, b.hist + 3 * kRadix,
+                                              b.status + (size_t)3 * tiles * kRadix, b.counters + 3, b.err);
+  k_gather_codes<<<ge, 256, 0, st>>>(b.vals_a, b.codes0, N, b.keys_b);
+  if (b.NI > 0)
+    k_hierarchy_batch<<<(b.NI + 255) / 256, 256, 0, st>>>(b.keys_b, b.tri_off, M, b.NI, b.nodes, b.parent, b.flags);
+  k_refit_batch<<<(N + kRefitBlock - 1) / kRefitBlock, kRefitBlock, 0, st>>>(
+      b.verts, b.vidx, b.vals_a, b.mesh_of, b.tri_off, N, b.NI, b.nodes, b.leaves, b.parent, b.flags, b.g);
   return cudaGetLastError();
 }
 

@@ -340,9 +340,37 @@ __device__ __forceinline__ float prune_bound(double best, float tau) {
 struct TravStats {
   uint32_t nodes = 0, tris = 0;
 };
-template <bool ANY, bool STATS = false>
+// The traversal stack: entries live in local memory, or (SHORT > 0) the top
+// SHORT entries in a per-thread shared-memory ring (slot i of thread t at
+// ring[i * blockDim.x]) with older entries spilled to local memory.
+template <int SHORT>
+struct TravStack {
+  int2 local[kStackSize];
+  int2* ring;
+  int sp = 0;
+  __device__ __forceinline__ void push(int2 e) {
+    if (SHORT == 0) {
+      local[sp++] = e;
+      return;
+    }
+    const int slot = (sp & (SHORT - 1)) * (int)blockDim.x;
+    if (sp >= SHORT) local[sp - SHORT] = ring[slot];
+    ring[slot] = e;
+    sp++;
+  }
+  __device__ __forceinline__ int2 pop() {
+    --sp;
+    if (SHORT == 0) return local[sp];
+    const int slot = (sp & (SHORT - 1)) * (int)blockDim.x;
+    const int2 e = ring[slot];
+    if (sp >= SHORT) ring[slot] = local[sp - SHORT];
+    return e;
+  }
+};
+
+template <bool ANY, bool STATS = false, int SHORT = 0>
 __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, float rb[6], HitRec& h,
-                                        TravStats* ts = nullptr) {
+                                        TravStats* ts = nullptr, int2* ring = nullptr) {
   if (S.ntri <= 0) return 0;
   float tp;
   if (!box_cons(r, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], tp)) return 0;
@@ -350,8 +378,8 @@ __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, float rb
   if (node < 0 && !leaf_box(r, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5])) return 0;
   bool have = false;
   float pb = __int_as_float(0x7f800000);  // prune bound; +inf until a hit
-  int2 stack[kStackSize];
-  int sp = 0;
+  TravStack<SHORT> stk;
+  stk.ring = ring;
   // a valid tree visits each node at most once per ray; the bound and the
   // index checks only guard against a corrupt tree
   const int64_t max_steps = 2 * (int64_t)S.ntri + 64;
@@ -373,8 +401,8 @@ __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, float rb
       }
       if (hl) {
         if (hr) {
-          if (sp >= kStackSize) return -1;
-          stack[sp++] = make_int2(ch.y, __float_as_int(tr));
+          if (stk.sp >= kStackSize) return -1;
+          stk.push(make_int2(ch.y, __float_as_int(tr)));
         }
         node = ch.x;
         continue;
@@ -405,8 +433,8 @@ __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, float rb
     }
     // pop
     bool next = false;
-    while (sp > 0) {
-      const int2 e = stack[--sp];
+    while (stk.sp > 0) {
+      const int2 e = stk.pop();
       if (!ANY && __int_as_float(e.y) > pb) continue;
       node = e.x;
       next = true;

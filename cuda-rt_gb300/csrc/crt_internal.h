@@ -42,7 +42,27 @@ struct MeshBufs {
   DMat* mats = nullptr;
 };
 
+// Many meshes in concatenated arrays (see build.cu, "batched").
+struct BatchBufs {
+  int M = 0, N = 0, NI = 0;  // meshes, triangles, internal nodes (N - M)
+  const float* verts = nullptr;
+  const int* vidx = nullptr;  // global vertex indices
+  const int* mesh_of = nullptr;
+  const int* tri_off = nullptr;  // M + 1
+  uint32_t *keys_a = nullptr, *keys_b = nullptr, *vals_a = nullptr, *vals_b = nullptr, *codes0 = nullptr;
+  uint32_t* hist = nullptr;    // 4 * kRadix
+  uint32_t* status = nullptr;  // 4 * tiles * kRadix
+  uint32_t* parent = nullptr;  // NI + N
+  int* flags = nullptr;        // NI
+  BNode* nodes = nullptr;      // NI (child codes local to each mesh)
+  LeafTri* leaves = nullptr;   // N
+  SceneGlobals* g = nullptr;   // M
+  unsigned* counters = nullptr;  // 4
+  int* err = nullptr;
+};
+
 int num_sms();
+cudaError_t launch_build_batch(const BatchBufs& b, cudaStream_t st);
 
 // build.cu
 cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st);
@@ -79,6 +99,28 @@ struct RenderArgs {
   double* grad_albedo = nullptr;
 };
 cudaError_t launch_render(const DScene& S, const RenderArgs& a, cudaStream_t st);
+
+// Device view of a batch for the batched pixel kernel.
+struct BatchView {
+  int M = 0, items = 0;
+  const int* item_off = nullptr;  // M + 1: first work item (pixel tile) of each mesh
+  const int* tri_off = nullptr;   // M + 1
+  const float* verts = nullptr;
+  const float* normals = nullptr;
+  const int* vidx = nullptr;
+  const int* nidx = nullptr;
+  const int* matid = nullptr;
+  const DMat* mats = nullptr;
+  const BNode* nodes = nullptr;
+  const LeafTri* leaves = nullptr;
+  SceneGlobals* g = nullptr;
+  const RenderArgs* args = nullptr;  // M
+  unsigned* counter = nullptr;
+};
+struct BatchTuning {
+  int block = 128, tw = 8, th = 4, stack = 0;
+};
+cudaError_t launch_render_batch(const BatchView& v, const BatchTuning& t, cudaStream_t st);
 cudaError_t launch_trace(const DScene& S, const double* rays, int64_t n, bool any, int* ids, double* t,
                          double* normals, cudaStream_t st);
 

@@ -56,26 +56,11 @@ __device__ __forceinline__ void warp_add(double* dst, double v) {
 // the forward and the adjoint) and accumulates d loss / d (vertices, light
 // position, albedo) for the Lambert and distance terms; visibility (which
 // triangle is hit, whether the shadow ray is blocked) is held fixed.
-template <int MODE>
-__global__ void __launch_bounds__(128, 4) k_pixels(DScene S, RenderArgs A) {
-  TravStats ts;
-  float rb[6], B, D;
-  scene_consts(S, rb, B, D);
-  const int lane = threadIdx.x & 31;
-  const int tiles_x = (A.W + kTileW - 1) / kTileW;
-  const int tiles_y = (A.row1 - A.row0 + kTileH - 1) / kTileH;
-  const int ntiles = tiles_x * tiles_y;
-  const int gx = (A.W + 15) / 16;  // gridDim.x of the reference's 16x16 launch
-  const D3 lpos = d3(A.lpos[0], A.lpos[1], A.lpos[2]);
-  D3 glight = d3(0, 0, 0);
-  while (true) {
-    int tile = 0;
-    if (lane == 0) tile = (int)atomicAdd(A.counter, 1u);
-    tile = __shfl_sync(0xffffffffu, tile, 0);
-    if (tile >= ntiles) break;
-    const int px = (tile % tiles_x) * kTileW + (lane % kTileW);
-    const int py = A.row0 + (tile / tiles_x) * kTileH + (lane / kTileW);
-    if (px >= A.W || py >= A.row1) continue;
+template <int MODE, int SHORT = 0>
+__device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int px, int py, float rb[6], float B,
+                                      float D, TravStats& ts, D3& glight, int2* ring = nullptr) {
+    const int gx = (A.W + 15) / 16;  // gridDim.x of the reference's 16x16 launch
+    const D3 lpos = d3(A.lpos[0], A.lpos[1], A.lpos[2]);
     const int idx = (A.H - py - 1) * A.W + px;
     // getGlobalIdx_2D_2D (inc/indexing.h:4-9) of the pixel's thread in the
     // reference launch, seeded by initPNRG (kernels/mrand.cu:38-41).
@@ -111,7 +96,7 @@ __global__ void __launch_bounds__(128, 4) k_pixels(DScene S, RenderArgs A) {
       RayC rc;
       ray_setup(rc, org.x, org.y, org.z, dir.x, dir.y, dir.z, B, D);
       HitRec h;
-      const int res = traverse<false, MODE == kRenderStats>(S, rc, rb, h, &ts);
+      const int res = traverse<false, MODE == kRenderStats, SHORT>(S, rc, rb, h, &ts, ring);
       if (res < 0) atomicOr(&S.g->err, kErrStack);
       D3 col;
       int sh = -1, shid = -1;
@@ -147,7 +132,7 @@ __global__ void __launch_bounds__(128, 4) k_pixels(DScene S, RenderArgs A) {
         RayC sr;
         ray_setup(sr, q.x, q.y, q.z, L.x, L.y, L.z, B, D);
         HitRec s;
-        const int sres = traverse<true, MODE == kRenderStats>(S, sr, rb, s, &ts);
+        const int sres = traverse<true, MODE == kRenderStats, SHORT>(S, sr, rb, s, &ts, ring);
         if (sres < 0) atomicOr(&S.g->err, kErrStack);
         sh = 0;
         int omid = -1;
@@ -251,7 +236,7 @@ __global__ void __launch_bounds__(128, 4) k_pixels(DScene S, RenderArgs A) {
         if (A.shadow_id) A.shadow_id[si] = shid;
       }
     }
-    if (MODE == kAdjoint) continue;
+    if (MODE == kAdjoint) return;
     const double inv = (double)A.spp;
     acc = d3(acc.x / inv, acc.y / inv, acc.z / inv);
     if (A.rgbf) {
@@ -275,7 +260,10 @@ __global__ void __launch_bounds__(128, 4) k_pixels(DScene S, RenderArgs A) {
         A.rgb8[3 * (int64_t)idx + ch] = (uint8_t)(255.0 * v);
       }
     }
-  }
+}
+
+template <int MODE>
+__device__ __forceinline__ void flush_stats(const RenderArgs& A, const TravStats& ts, const D3& glight) {
   if (MODE == kRenderStats) {
     unsigned long long a = ts.nodes, b = ts.tris;
 #pragma unroll
@@ -283,7 +271,7 @@ __global__ void __launch_bounds__(128, 4) k_pixels(DScene S, RenderArgs A) {
       a += __shfl_xor_sync(0xffffffffu, a, o);
       b += __shfl_xor_sync(0xffffffffu, b, o);
     }
-    if (lane == 0) {
+    if ((threadIdx.x & 31) == 0) {
       atomicAdd(A.stats, a);
       atomicAdd(A.stats + 1, b);
     }
@@ -292,6 +280,80 @@ __global__ void __launch_bounds__(128, 4) k_pixels(DScene S, RenderArgs A) {
     warp_add(A.grad_light, glight.x);
     warp_add(A.grad_light + 1, glight.y);
     warp_add(A.grad_light + 2, glight.z);
+  }
+}
+
+// One scene: warps claim 8x4-pixel tiles of rows [row0, row1).
+template <int MODE>
+__global__ void __launch_bounds__(128, 4) k_pixels(DScene S, RenderArgs A) {
+  TravStats ts;
+  D3 glight = d3(0, 0, 0);
+  float rb[6], B, D;
+  scene_consts(S, rb, B, D);
+  const int lane = threadIdx.x & 31;
+  const int tiles_x = (A.W + kTileW - 1) / kTileW;
+  const int tiles_y = (A.row1 - A.row0 + kTileH - 1) / kTileH;
+  const int ntiles = tiles_x * tiles_y;
+  while (true) {
+    int tile = 0;
+    if (lane == 0) tile = (int)atomicAdd(A.counter, 1u);
+    tile = __shfl_sync(0xffffffffu, tile, 0);
+    if (tile >= ntiles) break;
+    const int px = (tile % tiles_x) * kTileW + (lane % kTileW);
+    const int py = A.row0 + (tile / tiles_x) * kTileH + (lane / kTileW);
+    if (px >= A.W || py >= A.row1) continue;
+    pixel<MODE>(S, A, px, py, rb, B, D, ts, glight);
+  }
+  flush_stats<MODE>(A, ts, glight);
+}
+
+// Many scenes in one launch: work item i is (mesh, tile), with per-mesh tile
+// prefix sums item_off[M+1]; the warp's pixel tile is tw x th (tw * th = 32);
+// SHORT is the shared-memory part of the traversal stack (0: all local).
+template <int SHORT>
+__global__ void __launch_bounds__(256, 2) k_pixels_batch(BatchView V, int tw, int th) {
+  extern __shared__ int2 s_ring[];
+  int2* ring = SHORT > 0 ? s_ring + threadIdx.x : nullptr;
+  TravStats ts;
+  D3 glight = d3(0, 0, 0);
+  const int lane = threadIdx.x & 31;
+  int cur = -1;
+  DScene S;
+  RenderArgs A;
+  float rb[6], B = 0.f, D = 0.f;
+  while (true) {
+    int item = 0;
+    if (lane == 0) item = (int)atomicAdd(V.counter, 1u);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= V.items) break;
+    // mesh of this item: last m with item_off[m] <= item
+    int lo = 0, hi = V.M - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(V.item_off + mid) <= item)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const int m = lo;
+    if (m != cur) {
+      cur = m;
+      const int t0 = __ldg(V.tri_off + m), n = __ldg(V.tri_off + m + 1) - t0;
+      S.ntri = n;
+      S.root = n >= 2 ? 0 : ~0;
+      S.verts = V.verts, S.normals = V.normals, S.vidx = V.vidx, S.nidx = V.nidx, S.matid = V.matid, S.mats = V.mats;
+      S.nodes = V.nodes + (t0 - m);
+      S.leaves = V.leaves + t0;
+      S.g = V.g + m;
+      A = V.args[m];
+      scene_consts(S, rb, B, D);
+    }
+    const int tile = item - __ldg(V.item_off + m);
+    const int tiles_x = (A.W + tw - 1) / tw;
+    const int px = (tile % tiles_x) * tw + (lane % tw);
+    const int py = (tile / tiles_x) * th + (lane / tw);
+    if (px >= A.W || py >= A.H) continue;
+    pixel<kRender, SHORT>(S, A, px, py, rb, B, D, ts, glight, ring);
   }
 }
 
@@ -311,6 +373,27 @@ cudaError_t launch_render(const DScene& S, const RenderArgs& a, cudaStream_t st)
     k_pixels<kRender><<<num_sms() * (bps > 0 ? bps : 1), 128, 0, st>>>(S, a);
   }
   return cudaGetLastError();
+}
+
+template <int SHORT>
+static cudaError_t launch_batch_t(const BatchView& v, int block, int tw, int th, cudaStream_t st) {
+  const size_t smem = (size_t)SHORT * block * sizeof(int2);
+  int bps = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_pixels_batch<SHORT>, block, smem);
+  k_pixels_batch<SHORT><<<num_sms() * (bps > 0 ? bps : 1), block, smem, st>>>(v, tw, th);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_render_batch(const BatchView& v, const BatchTuning& t, cudaStream_t st) {
+  cudaMemsetAsync(v.counter, 0, sizeof(unsigned), st);
+  switch (t.stack) {
+    case 8:
+      return launch_batch_t<8>(v, t.block, t.tw, t.th, st);
+    case 16:
+      return launch_batch_t<16>(v, t.block, t.tw, t.th, st);
+    default:
+      return launch_batch_t<0>(v, t.block, t.tw, t.th, st);
+  }
 }
 
 cudaError_t launch_trace(const DScene& S, const double* rays, int64_t n, bool any, int* ids, double* t,

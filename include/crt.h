@@ -210,6 +210,53 @@ crt_status crt_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* vals_
  * recorded (stack overflow, bounded-wait timeout, non-finite input). */
 crt_status crt_scene_check(crt_scene* scene, void* stream);
 
+/* ---- batched form: no counterpart in the reference, whose main loop
+ * (src/main.cpp:300-330) builds and renders one mesh per process.  Many
+ * meshes, each with its own camera, light and image size, are built by one
+ * sequence of segmented kernels (the same Morton codes, sort, split search
+ * and refit as crt_bvh_build, per mesh) and rendered by one persistent launch
+ * whose warps claim (mesh, pixel tile) work items; crt_batch_run captures
+ * that sequence once into a CUDA graph and replays it.  Every mesh's image
+ * is what crt_render gives for that mesh alone. */
+typedef struct crt_batch crt_batch;
+
+typedef struct crt_batch_view {
+  crt_camera camera;
+  crt_light light;
+  int32_t width, height, spp;
+} crt_batch_view;
+
+/* Launch shape of the batched pixel kernel: block_size in {64, 128, 256};
+ * tile_w x tile_h = 32 pixels of one warp (8x4, 4x8, 16x2, 32x1); stack =
+ * traversal-stack entries kept in shared memory per thread (0, 8, 16), the
+ * rest of the 64 in local memory. */
+typedef struct crt_batch_tuning {
+  int32_t block_size, tile_w, tile_h, stack;
+  float render_ms; /* written by crt_batch_autotune: the chosen shape's render time */
+} crt_batch_tuning;
+
+/* Host meshes and views (num_meshes <= 1024).  Copies everything to one
+ * device allocation, including the concatenated rgb8 images (mesh m's image
+ * follows mesh m-1's, each in crt_render_out's bottom-up order). */
+crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* views, int32_t num_meshes,
+                            void* stream, crt_batch** out);
+crt_status crt_batch_destroy(crt_batch* batch);
+/* Build every mesh's BVH and render every view.  use_graph != 0 replays a
+ * CUDA graph of the whole sequence (captured on the first such call after
+ * create or a tuning change).  rgb8 (host or device, NULL to skip) receives
+ * the concatenated images; a host rgb8 synchronises `stream`. */
+crt_status crt_batch_run(crt_batch* batch, int32_t use_graph, uint8_t* rgb8, void* stream);
+crt_status crt_batch_set_tuning(crt_batch* batch, const crt_batch_tuning* tuning);
+/* Times the render under each of the 36 supported tunings (one warm-up and
+ * one timed launch each, after one build) and keeps the fastest. */
+crt_status crt_batch_autotune(crt_batch* batch, crt_batch_tuning* chosen, void* stream);
+/* Mesh `mesh`'s build products in crt_bvh_export's layout (host or device
+ * pointers; any may be NULL).  Synchronises `stream`. */
+crt_status crt_batch_export(crt_batch* batch, int32_t mesh, float* scene_box, int32_t* codes, uint32_t* ids,
+                            int32_t* nodes3, float* node_boxes, void* stream);
+/* Synchronise `stream` and report device-side errors of the last run. */
+crt_status crt_batch_check(crt_batch* batch, void* stream);
+
 const char* crt_last_error_string(void);
 const char* crt_version(void);
 
