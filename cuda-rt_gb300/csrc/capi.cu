@@ -484,7 +484,7 @@ crt_status crt_adjoint_lambert(crt_scene* s, const crt_camera* cam, const crt_li
   a.counter = s->counter;
   a.rgb8 = nullptr, a.rgbf = nullptr, a.hit_id = nullptr, a.hit_t = nullptr, a.shadow = nullptr, a.rays = nullptr;
   a.stats = nullptr;
-  DevView vg, vgd, vv, vl, vk;
+  DevView vg, vgd;
   CRT_CUDA(vg.open(const_cast<double*>(grad_rgb), 3 * sizeof(double) * npx, true, st), "stage grad_rgb");
   CRT_CUDA(vgd.open(const_cast<double*>(grad_depth), sizeof(double) * npx, true, st), "stage grad_depth");
   // gradient outputs: always through device scratch (they are accumulated atomically)

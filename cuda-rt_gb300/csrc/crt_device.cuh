@@ -226,13 +226,6 @@ static __device__ __noinline__ bool box_exact(double ox, double oy, double oz, d
   return tMin <= tMax;
 }
 
-// A leaf box: the exact answer, in float when the filters are certain.
-__device__ __forceinline__ bool leaf_box(const RayC& r, float lox, float hix, float loy, float hiy, float loz,
-                                         float hiz) {
-  return box_sure(r, lox, hix, loy, hiy, loz, hiz) ||
-         box_exact(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, lox, hix, loy, hiy, loz, hiz);
-}
-
 // Certain rejection for the triangle test (tri_exact): true only when the
 // double Moller-Trumbore test certainly rejects.  The FP32 determinant and
 // numerators differ from the exact values by at most
@@ -368,81 +361,124 @@ struct TravStack {
   }
 };
 
+// Leaf codes carry a flag: bit 30 of ~code set = the leaf's box passed the
+// conservative filter but not the certain one, so its exact box test is
+// still due.  kPop marks "take the next node from the stack".
+constexpr int kLeafBoxDue = 1 << 30;
+constexpr int kLeafIndex = kLeafBoxDue - 1;
+constexpr int kPop = (int)0x80000000;
+
+// Warp-synchronous traversal: all 32 lanes of the warp call it together
+// (`live` false: the lane has no ray and only takes part in the votes).
+// Each round, every lane walks its own stack in FP32 until it reaches its
+// next candidate leaf (box filter passed, triangle not certainly rejected)
+// or runs out of nodes; then the lanes holding a candidate run the exact
+// double tests together.  The double arithmetic is thus issued once per
+// round for the whole warp instead of once per lane.  A lane waits at its
+// candidate until it is tested, so candidates are tested one at a time in
+// left-first DFS order, each against the best hit so far, and the pruning
+// bound is current when the lane walks on: the result and the visited nodes
+// are those of the sequential traversal.
 template <bool ANY, bool STATS = false, int SHORT = 0>
-__device__ __forceinline__ int traverse(const DScene& S, const RayC& r, float rb[6], HitRec& h,
+__device__ __forceinline__ int traverse(const DScene& S, const RayC& r, const float rb[6], HitRec& h, bool live,
                                         TravStats* ts = nullptr, int2* ring = nullptr) {
-  if (S.ntri <= 0) return 0;
+  bool run = live && S.ntri > 0;
+  bool have = false, err = false;
   float tp;
-  if (!box_cons(r, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], tp)) return 0;
+  if (run && !box_cons(r, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], tp)) run = false;
   int node = S.root;
-  if (node < 0 && !leaf_box(r, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5])) return 0;
-  bool have = false;
+  if (node < 0 && !box_sure(r, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5])) node = ~kLeafBoxDue;
   float pb = __int_as_float(0x7f800000);  // prune bound; +inf until a hit
   TravStack<SHORT> stk;
   stk.ring = ring;
+  int cand = 0;  // the pending candidate's leaf code (with its box flag)
+  bool pending = false;
   // a valid tree visits each node at most once per ray; the bound and the
   // index checks only guard against a corrupt tree
   const int64_t max_steps = 2 * (int64_t)S.ntri + 64;
-  for (int64_t steps = 0;; steps++) {
-    if (steps > max_steps || node >= S.ntri - 1 || ~node >= S.ntri) return -1;
-    if (node >= 0) {
-      if (STATS) ts->nodes++;
-      const float4* np = reinterpret_cast<const float4*>(S.nodes + node);
-      const float4 xl = __ldg(np + 0), xr = __ldg(np + 1), zz = __ldg(np + 2);
-      const int4 ch = __ldg(reinterpret_cast<const int4*>(np + 3));
-      float tl, tr;
-      bool hl = box_cons(r, xl.x, xl.y, xl.z, xl.w, zz.x, zz.y, tl);
-      bool hr = box_cons(r, xr.x, xr.y, xr.z, xr.w, zz.z, zz.w, tr);
-      if (hl && ch.x < 0) hl = leaf_box(r, xl.x, xl.y, xl.z, xl.w, zz.x, zz.y);
-      if (hr && ch.y < 0) hr = leaf_box(r, xr.x, xr.y, xr.z, xr.w, zz.z, zz.w);
-      if (!ANY) {
-        hl = hl && !(tl > pb);
-        hr = hr && !(tr > pb);
-      }
-      if (hl) {
-        if (hr) {
-          if (stk.sp >= kStackSize) return -1;
-          stk.push(make_int2(ch.y, __float_as_int(tr)));
+  int64_t steps = 0;
+  while (true) {
+    // FP32 phase: this lane's next candidate
+    while (run && !pending) {
+      if (node == kPop) {
+        bool next = false;
+        while (stk.sp > 0) {
+          const int2 e = stk.pop();
+          if (!ANY && __int_as_float(e.y) > pb) continue;
+          node = e.x;
+          next = true;
+          break;
         }
-        node = ch.x;
-        continue;
+        if (!next) {
+          run = false;
+          break;
+        }
       }
-      if (hr) {
-        node = ch.y;
-        continue;
+      if (++steps > max_steps || node >= S.ntri - 1 || (node < 0 && (~node & kLeafIndex) >= S.ntri)) {
+        err = true;
+        run = false;
+        break;
       }
-    } else {
-      if (STATS) ts->tris++;
-      const float4* lp = reinterpret_cast<const float4*>(S.leaves + (~node));
+      if (node >= 0) {
+        if (STATS) ts->nodes++;
+        const float4* np = reinterpret_cast<const float4*>(S.nodes + node);
+        const float4 xl = __ldg(np + 0), xr = __ldg(np + 1), zz = __ldg(np + 2);
+        const int4 ch = __ldg(reinterpret_cast<const int4*>(np + 3));
+        float tl, tr;
+        bool hl = box_cons(r, xl.x, xl.y, xl.z, xl.w, zz.x, zz.y, tl);
+        bool hr = box_cons(r, xr.x, xr.y, xr.z, xr.w, zz.z, zz.w, tr);
+        if (!ANY) {
+          hl = hl && !(tl > pb);
+          hr = hr && !(tr > pb);
+        }
+        int cl = ch.x, cr = ch.y;
+        if (hl && cl < 0 && !box_sure(r, xl.x, xl.y, xl.z, xl.w, zz.x, zz.y)) cl = ~(~cl | kLeafBoxDue);
+        if (hr && cr < 0 && !box_sure(r, xr.x, xr.y, xr.z, xr.w, zz.z, zz.w)) cr = ~(~cr | kLeafBoxDue);
+        if (hl) {
+          if (hr) {
+            if (stk.sp >= kStackSize) {
+              err = true;
+              run = false;
+              break;
+            }
+            stk.push(make_int2(cr, __float_as_int(tr)));
+          }
+          node = cl;
+        } else {
+          node = hr ? cr : kPop;
+        }
+      } else {
+        if (STATS) ts->tris++;
+        const float4* lp = reinterpret_cast<const float4*>(S.leaves + (~node & kLeafIndex));
+        const float4 a = __ldg(lp), b = __ldg(lp + 1), c = __ldg(lp + 2);
+        if (!tri_reject_sure(r, a, b, c)) cand = node, pending = true;
+        node = kPop;
+      }
+    }
+    // double phase: the lanes holding a candidate, together
+    if (__ballot_sync(0xffffffffu, pending) == 0u) break;
+    if (pending) {
+      const float4* lp = reinterpret_cast<const float4*>(S.leaves + (~cand & kLeafIndex));
       const float4 a = __ldg(lp), b = __ldg(lp + 1), c = __ldg(lp + 2);
-      TriHit th;
-      th.hit = false;
-      if (!tri_reject_sure(r, a, b, c)) th = tri_exact(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, a, b, c);
-      if (th.hit) {
-        const double t = th.t, al = th.alpha, be = th.beta;
-        if (ANY) {
-          h.t = t, h.alpha = al, h.beta = be, h.id = __float_as_int(a.w);
-          return 1;
-        }
-        if (!have || t < h.t) {
-          h.t = t, h.alpha = al, h.beta = be, h.id = __float_as_int(a.w);
+      bool in_box = true;
+      if (~cand & kLeafBoxDue) {  // the leaf's box, as the refit computes it from the same vertices
+        in_box = box_exact(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, fminf(c.x, fminf(a.x, b.x)),
+                           fmaxf(c.x, fmaxf(a.x, b.x)), fminf(c.y, fminf(a.y, b.y)), fmaxf(c.y, fmaxf(a.y, b.y)),
+                           fminf(c.z, fminf(a.z, b.z)), fmaxf(c.z, fmaxf(a.z, b.z)));
+      }
+      pending = false;
+      if (in_box) {
+        const TriHit th = tri_exact(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, a, b, c);
+        if (th.hit && (ANY || !have || th.t < h.t)) {
+          h.t = th.t, h.alpha = th.alpha, h.beta = th.beta, h.id = __float_as_int(a.w);
           have = true;
-          pb = prune_bound(t, r.tau);
+          if (ANY) run = false;
+          else pb = prune_bound(th.t, r.tau);
         }
       }
     }
-    // pop
-    bool next = false;
-    while (stk.sp > 0) {
-      const int2 e = stk.pop();
-      if (!ANY && __int_as_float(e.y) > pb) continue;
-      node = e.x;
-      next = true;
-      break;
-    }
-    if (!next) break;
   }
-  return have ? 1 : 0;
+  return err ? -1 : (have ? 1 : 0);
 }
 
 // The scene constants the ray setup needs: B = max |coordinate| of the root

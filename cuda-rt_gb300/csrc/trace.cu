@@ -21,13 +21,23 @@ __global__ void __launch_bounds__(128) k_trace(DScene S, const double* __restric
                                                double* __restrict__ nout) {
   float rb[6], B, D;
   scene_consts(S, rb, B, D);
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double* r = rays + 6 * i;
+  const int lane = threadIdx.x & 31;
+  // warp-uniform loop (the traversal is warp-synchronous): lanes past n ride along
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
+    const int64_t i = base + lane;
+    const bool live = i < n;
     RayC rc;
-    ray_setup(rc, r[0], r[1], r[2], r[3], r[4], r[5], B, D);
+    if (live) {
+      const double* r = rays + 6 * i;
+      ray_setup(rc, r[0], r[1], r[2], r[3], r[4], r[5], B, D);
+    } else {
+      ray_setup(rc, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0, B, D);
+    }
     HitRec h;
-    const int res = traverse<ANY>(S, rc, rb, h);
+    const int res = traverse<ANY>(S, rc, rb, h, live);
     if (res < 0) atomicOr(&S.g->err, kErrStack);
+    if (!live) continue;
     const bool hit = res > 0;
     ids[i] = hit ? h.id : -1;
     if (tout) tout[i] = hit ? h.t : 0.0;
@@ -56,9 +66,15 @@ __device__ __forceinline__ void warp_add(double* dst, double v) {
 // the forward and the adjoint) and accumulates d loss / d (vertices, light
 // position, albedo) for the Lambert and distance terms; visibility (which
 // triangle is hit, whether the shadow ray is blocked) is held fixed.
+//
+// All 32 lanes of the warp call it together, each with its own pixel (valid
+// false: a lane outside the image, which computes nothing and writes
+// nothing); sample k of every lane is traced by one warp-synchronous
+// traversal, so the double arithmetic of ray generation, exact tests and
+// shading is issued for the warp's lanes together.
 template <int MODE, int SHORT = 0>
-__device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int px, int py, float rb[6], float B,
-                                      float D, TravStats& ts, D3& glight, int2* ring = nullptr) {
+__device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int px, int py, bool valid, float rb[6],
+                                      float B, float D, TravStats& ts, D3& glight, int2* ring = nullptr) {
     const int gx = (A.W + 15) / 16;  // gridDim.x of the reference's 16x16 launch
     const D3 lpos = d3(A.lpos[0], A.lpos[1], A.lpos[2]);
     const int idx = (A.H - py - 1) * A.W + px;
@@ -68,11 +84,14 @@ __device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int 
     uint32_t st = wang_hash(gid);
     const double xx = (2 * ((px + 0.5) * A.invW) - 1) * A.angle * A.aspect;
     const double yy = (1 - 2 * ((py + 0.5) * A.invH)) * A.angle;
+    // the pinhole direction scaled to the focal plane: the same for every sample
+    D3 fdir = normalize_exact(d3(xx, yy, -1.0));
+    fdir = d3(fdir.x * A.focal, fdir.y * A.focal, fdir.z * A.focal);
     D3 acc = d3(0, 0, 0);
     double depth = 0.0;
     D3 G = d3(0, 0, 0);
     double Gd = 0.0;
-    if (MODE == kAdjoint) {
+    if (MODE == kAdjoint && valid) {
       const double inv = 1.0 / (double)A.spp;
       G = d3(A.grad_rgb[3 * (int64_t)idx] * inv, A.grad_rgb[3 * (int64_t)idx + 1] * inv,
              A.grad_rgb[3 * (int64_t)idx + 2] * inv);
@@ -86,59 +105,66 @@ __device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int 
       if (dofRadius != 0.0) {  // a zero radius gives +-0 components, which no later operation can tell apart
         org = d3(dofRadius * cos(dofAngle), dofRadius * sin(dofAngle), 0.0);
       }
-      D3 dir = normalize_exact(d3(xx, yy, -1.0));
-      dir = d3(dir.x * A.focal, dir.y * A.focal, dir.z * A.focal) - org;
-      dir = normalize_exact(dir);
-      if (MODE != kAdjoint && A.rays) {
+      const D3 dir = normalize_exact(fdir - org);
+      if (MODE != kAdjoint && A.rays && valid) {
         double* rr = A.rays + 6 * si;
         rr[0] = org.x, rr[1] = org.y, rr[2] = org.z, rr[3] = dir.x, rr[4] = dir.y, rr[5] = dir.z;
       }
       RayC rc;
       ray_setup(rc, org.x, org.y, org.z, dir.x, dir.y, dir.z, B, D);
       HitRec h;
-      const int res = traverse<false, MODE == kRenderStats, SHORT>(S, rc, rb, h, &ts, ring);
+      const int res = traverse<false, MODE == kRenderStats, SHORT>(S, rc, rb, h, valid, &ts, ring);
       if (res < 0) atomicOr(&S.g->err, kErrStack);
-      D3 col;
-      int sh = -1, shid = -1;
-      if (res > 0) {
-        const D3 q = org + (h.t * dir);
-        const int mid = __ldg(S.matid + h.id);
-        const DMat m = S.mats[mid];
+      const bool hit = valid && res > 0;
+      // traceRay up to the shadow ray (lanes with a hit)
+      D3 q, N, V, L;
+      double sN = 0.0, sL = 0.0, dist = 0.0, fall = 0.0, datt = 0.0;
+      bool tiny = false;
+      RayC sr;
+      if (hit) {
+        q = org + (h.t * dir);
         // smooth normal, bvh.cu:357-364 (hit_normal, kept apart for the adjoint)
         const int na = S.nidx[3 * h.id], nb = S.nidx[3 * h.id + 1], nc = S.nidx[3 * h.id + 2];
         const D3 nA = d3(S.normals[3 * na], S.normals[3 * na + 1], S.normals[3 * na + 2]);
         const D3 nB = d3(S.normals[3 * nb], S.normals[3 * nb + 1], S.normals[3 * nb + 2]);
         const D3 nC = d3(S.normals[3 * nc], S.normals[3 * nc + 1], S.normals[3 * nc + 2]);
         const D3 Nr = (1.0 - (h.alpha + h.beta)) * nA + h.alpha * nB + h.beta * nC;
-        const double sN = 1.0 / (double)sqrtf(__double2float_rn(Nr.x * Nr.x + Nr.y * Nr.y + Nr.z * Nr.z));
-        const D3 N = d3(Nr.x * sN, Nr.y * sN, Nr.z * sN);
-        D3 I = d3(m.ke[0] + m.ka[0] * 0.0, m.ke[1] + m.ka[1] * 0.0, m.ke[2] + m.ka[2] * 0.0);
-        D3 V = d3(A.eye[0], A.eye[1], A.eye[2]) - q;
+        sN = 1.0 / (double)sqrtf(__double2float_rn(Nr.x * Nr.x + Nr.y * Nr.y + Nr.z * Nr.z));
+        N = d3(Nr.x * sN, Nr.y * sN, Nr.z * sN);
+        V = d3(A.eye[0], A.eye[1], A.eye[2]) - q;
         V = normalize_exact(d3(-V.x, -V.y, -V.z));
         // Light::getDirection: three draws (x, y, z), times radius, minus 0.5
         const double r0 = rand_double(st), r1 = rand_double(st), r2 = rand_double(st);
         const D3 off = d3(r0 * A.lradius - 0.5, r1 * A.lradius - 0.5, r2 * A.lradius - 0.5);
         const D3 Lp = lpos + off - q;
-        const double sL = 1.0 / (double)sqrtf(__double2float_rn(Lp.x * Lp.x + Lp.y * Lp.y + Lp.z * Lp.z));
-        const D3 L = d3(Lp.x * sL, Lp.y * sL, Lp.z * sL);
+        sL = 1.0 / (double)sqrtf(__double2float_rn(Lp.x * Lp.x + Lp.y * Lp.y + Lp.z * Lp.z));
+        L = d3(Lp.x * sL, Lp.y * sL, Lp.z * sL);
         // Light::distanceAttenuation
-        const double dist = norm_exact(lpos - q);
-        double fall = A.latt[0] + (A.latt[1] + A.latt[2] * dist) * dist;
-        const bool tiny = fabs(fall) < kRayEps;
+        dist = norm_exact(lpos - q);
+        fall = A.latt[0] + (A.latt[1] + A.latt[2] * dist) * dist;
+        tiny = fabs(fall) < kRayEps;
         fall = tiny ? 1.0 : 1.0 / fall;
-        const double datt = fmin(1.0, fall);
-        // Light::shadowAttenuation: any-hit from q towards the light
-        D3 satt = d3(1, 1, 1);
-        RayC sr;
+        datt = fmin(1.0, fall);
         ray_setup(sr, q.x, q.y, q.z, L.x, L.y, L.z, B, D);
-        HitRec s;
-        const int sres = traverse<true, MODE == kRenderStats, SHORT>(S, sr, rb, s, &ts, ring);
-        if (sres < 0) atomicOr(&S.g->err, kErrStack);
+      } else {
+        ray_setup(sr, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0, B, D);
+      }
+      // Light::shadowAttenuation: any-hit from q towards the light
+      HitRec s;
+      const int sres = traverse<true, MODE == kRenderStats, SHORT>(S, sr, rb, s, hit, &ts, ring);
+      if (sres < 0) atomicOr(&S.g->err, kErrStack);
+      D3 col = d3(0.9, 0.9, 0.9);
+      int sh = -1, shid = -1;
+      if (hit) {
+        const int mid = __ldg(S.matid + h.id);
+        const DMat m = S.mats[mid];
+        D3 I = d3(m.ke[0] + m.ka[0] * 0.0, m.ke[1] + m.ka[1] * 0.0, m.ke[2] + m.ka[2] * 0.0);
+        D3 satt = d3(1, 1, 1);
         sh = 0;
         int omid = -1;
         bool otrans = false;
         DMat om;
-        if (sres > 0 && s.t < norm_exact(lpos - q) && !(s.t < kRayEps)) {
+        if (sres > 0 && s.t < dist && !(s.t < kRayEps)) {  // dist = norm(lpos - q), Light.cu:14-16
           sh = 1;
           shid = s.id;
           omid = __ldg(S.matid + s.id);
@@ -195,6 +221,10 @@ __device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int 
           glight = glight + gP;
           const D3 gq = d3(-gP.x, -gP.y, -gP.z);
           // lam through N = Nr / |Nr|, Nr = (1-a-b) nA + a nB + b nC
+          const int na = S.nidx[3 * h.id], nb = S.nidx[3 * h.id + 1], nc = S.nidx[3 * h.id + 2];
+          const D3 nA = d3(S.normals[3 * na], S.normals[3 * na + 1], S.normals[3 * na + 2]);
+          const D3 nB = d3(S.normals[3 * nb], S.normals[3 * nb + 1], S.normals[3 * nb + 2]);
+          const D3 nC = d3(S.normals[3 * nc], S.normals[3 * nc + 1], S.normals[3 * nc + 2]);
           const D3 gN = d3((L.x - NL * N.x) * sN * S_lam, (L.y - NL * N.y) * sN * S_lam,
                            (L.z - NL * N.z) * sN * S_lam);
           const double g_al = dot(gN, nB - nA), g_be = dot(gN, nC - nA);
@@ -225,18 +255,16 @@ __device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int 
           }
         }
         depth += h.t;
-      } else {
-        col = d3(0.9, 0.9, 0.9);
       }
       acc = acc + col;
-      if (MODE != kAdjoint) {
-        if (A.hit_id) A.hit_id[si] = res > 0 ? h.id : -1;
-        if (A.hit_t) A.hit_t[si] = res > 0 ? h.t : 0.0;
+      if (MODE != kAdjoint && valid) {
+        if (A.hit_id) A.hit_id[si] = hit ? h.id : -1;
+        if (A.hit_t) A.hit_t[si] = hit ? h.t : 0.0;
         if (A.shadow) A.shadow[si] = sh;
         if (A.shadow_id) A.shadow_id[si] = shid;
       }
     }
-    if (MODE == kAdjoint) return;
+    if (MODE == kAdjoint || !valid) return;
     const double inv = (double)A.spp;
     acc = d3(acc.x / inv, acc.y / inv, acc.z / inv);
     if (A.rgbf) {
@@ -301,8 +329,7 @@ __global__ void __launch_bounds__(128, 4) k_pixels(DScene S, RenderArgs A) {
     if (tile >= ntiles) break;
     const int px = (tile % tiles_x) * kTileW + (lane % kTileW);
     const int py = A.row0 + (tile / tiles_x) * kTileH + (lane / kTileW);
-    if (px >= A.W || py >= A.row1) continue;
-    pixel<MODE>(S, A, px, py, rb, B, D, ts, glight);
+    pixel<MODE>(S, A, px, py, px < A.W && py < A.row1, rb, B, D, ts, glight);
   }
   flush_stats<MODE>(A, ts, glight);
 }
@@ -352,8 +379,7 @@ __global__ void __launch_bounds__(256, 2) k_pixels_batch(BatchView V, int tw, in
     const int tiles_x = (A.W + tw - 1) / tw;
     const int px = (tile % tiles_x) * tw + (lane % tw);
     const int py = (tile / tiles_x) * th + (lane / tw);
-    if (px >= A.W || py >= A.H) continue;
-    pixel<kRender, SHORT>(S, A, px, py, rb, B, D, ts, glight, ring);
+    pixel<kRender, SHORT>(S, A, px, py, px < A.W && py < A.H, rb, B, D, ts, glight, ring);
   }
 }
 
