@@ -173,9 +173,9 @@ def run_crt(args, dist, rank, ws):
     value = rays * args.steps * ws / t_total / 1e6
     ms_step = t_total / args.steps * 1e3
     hbm, peak_kind = peaks()
-    # render roofline (the dominant kernel): 64 B per visited internal node +
-    # 36 B per tested triangle (the fixed traffic model), per launch
-    alg_bytes = nodes_visited * 64 + tris_tested * 36
+    # render roofline (the dominant kernel): the bytes the traversal fetches,
+    # 128 B per visited four-wide node + 48 B per tested leaf triangle, per launch
+    alg_bytes = nodes_visited * 128 + tris_tested * 48
     render_s = t_render / args.steps
     achieved = alg_bytes / render_s / 1e9
     build_s = t_build / args.steps

@@ -70,7 +70,7 @@ class _BatchView(C.Structure):
 
 
 class _BatchTuning(C.Structure):
-    _fields_ = [("block_size", C.c_int32), ("tile_w", C.c_int32), ("tile_h", C.c_int32), ("stack", C.c_int32),
+    _fields_ = [("block_size", C.c_int32), ("lanes_per_pixel", C.c_int32), ("stack", C.c_int32),
                 ("render_ms", C.c_float)]
 
 
@@ -325,14 +325,14 @@ class Batch:
         """Split run()'s concatenated output into per-mesh (W*H, 3) views."""
         return [out[self.offsets[m]:self.offsets[m + 1]] for m in range(self.M)]
 
-    def set_tuning(self, block_size, tile_w, tile_h, stack):
-        t = _BatchTuning(block_size, tile_w, tile_h, stack, 0.0)
+    def set_tuning(self, block_size, lanes_per_pixel, stack):
+        t = _BatchTuning(block_size, lanes_per_pixel, stack, 0.0)
         _check(lib().crt_batch_set_tuning(self.h, C.byref(t)))
 
     def autotune(self, stream=None):
         t = _BatchTuning()
         _check(lib().crt_batch_autotune(self.h, C.byref(t), _stream(stream)))
-        return dict(block_size=t.block_size, tile_w=t.tile_w, tile_h=t.tile_h, stack=t.stack,
+        return dict(block_size=t.block_size, lanes_per_pixel=t.lanes_per_pixel, stack=t.stack,
                     render_ms=float(t.render_ms))
 
     def check(self, stream=None):

@@ -10,7 +10,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/crt.h"
+#include "crt.h"
 #include "crt_internal.h"
 
 namespace crt {
@@ -22,7 +22,7 @@ using namespace crt;
 struct crt_batch {
   int M = 0, N = 0, V = 0, Nn = 0, Mat = 0;
   std::vector<int> tri_off, px_off;  // host copies
-  std::vector<int> item_off;           // kTileShapes x (M + 1): work-item prefix per tile shape
+  std::vector<int> item_off;           // kLaneOptions x (M + 1): work-item prefix per lanes option
   int* d_item_off = nullptr;
   std::vector<crt_batch_view> views;
   void* block = nullptr;  // one allocation for everything
@@ -64,19 +64,20 @@ bool on_device(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-constexpr int kTileShapes = 4;
-constexpr int kTileW[kTileShapes] = {8, 4, 16, 32};
+// Work-item prefixes are kept for every lanes-per-pixel option.
+constexpr int kLaneOptions = 6;
+constexpr int kLanes[kLaneOptions] = {1, 2, 4, 8, 16, 32};
 
-int shape_of(const BatchTuning& t) {
-  for (int s = 0; s < kTileShapes; s++)
-    if (kTileW[s] == t.tw) return s;
+int option_of(const BatchTuning& t) {
+  for (int s = 0; s < kLaneOptions; s++)
+    if (kLanes[s] == t.lanes) return s;
   return 0;
 }
 
-// The device view for tuning t (the work-item prefix depends on the tile shape).
+// The device view for tuning t (the work-item prefix depends on the lanes per pixel).
 BatchView view_for(const crt_batch* b, const BatchTuning& t) {
   BatchView v = b->v;
-  const int s = shape_of(t);
+  const int s = option_of(t);
   v.item_off = b->d_item_off + (size_t)s * (b->M + 1);
   v.items = b->item_off[(size_t)s * (b->M + 1) + b->M];
   return v;
@@ -109,7 +110,7 @@ crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* v
     delete b;
     return fail(CRT_INVALID_ARG, "at most " + std::to_string(kRadix) + " meshes in a batch");
   }
-  b->item_off.assign((size_t)kTileShapes * (M + 1), 0);
+  b->item_off.assign((size_t)kLaneOptions * (M + 1), 0);
   b->px_off.assign(M + 1, 0);
   std::vector<int> vert_off(M + 1, 0), nrm_off(M + 1, 0), mat_off(M + 1, 0);
   for (int m = 0; m < M; m++) {
@@ -140,8 +141,8 @@ crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* v
     vert_off[m + 1] = vert_off[m] + d.num_vertices;
     nrm_off[m + 1] = nrm_off[m] + d.num_normals;
     mat_off[m + 1] = mat_off[m] + d.num_materials;
-    for (int sh = 0; sh < kTileShapes; sh++) {  // warp tiles of 32 pixels
-      const int tw = kTileW[sh], th = 32 / tw;
+    for (int sh = 0; sh < kLaneOptions; sh++) {  // warp tiles of 32 / G pixels
+      const int G = lanes_per_pixel(w.spp, kLanes[sh]), tw = group_tile_w(G), th = group_tile_h(G);
       int* io = &b->item_off[(size_t)sh * (M + 1)];
       io[m + 1] = io[m] + ((w.width + tw - 1) / tw) * ((w.height + th - 1) / th);
     }
@@ -179,11 +180,11 @@ crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* v
   const int NI = N - M;
   b->image_bytes = 3 * (size_t)b->px_off[M];
   const size_t sz[] = {12 * (size_t)V, 12 * (size_t)Nn, 12 * (size_t)N, 12 * (size_t)N, 4 * (size_t)N,
-                       sizeof(DMat) * (size_t)Mat, 4 * (size_t)N, 4 * (size_t)(M + 1), 4 * (size_t)kTileShapes * (M + 1),
+                       sizeof(DMat) * (size_t)Mat, 4 * (size_t)N, 4 * (size_t)(M + 1), 4 * (size_t)kLaneOptions * (M + 1),
                        5 * 4 * (size_t)N, 4 * 4 * (size_t)kRadix, 4 * 4 * (size_t)tiles * kRadix,
                        4 * (size_t)(NI + N), 4 * (size_t)(NI > 0 ? NI : 1), sizeof(BNode) * (size_t)(NI > 0 ? NI : 1),
                        sizeof(LeafTri) * (size_t)N, sizeof(SceneGlobals) * (size_t)M, 64, b->image_bytes,
-                       sizeof(RenderArgs) * (size_t)M};
+                       sizeof(RenderArgs) * (size_t)M, sizeof(WNode) * (size_t)(NI > 0 ? NI : 1)};
   const int K = sizeof(sz) / sizeof(sz[0]);
   std::vector<size_t> off(K);
   size_t total = 0;
@@ -221,11 +222,12 @@ crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* v
   bb.err = (int*)(at(17) + 32);
   b->image = (uint8_t*)at(18);
   b->args = (RenderArgs*)at(19);
+  bb.wnodes = (WNode*)at(20);
   BatchView& v = b->v;
   b->d_item_off = d_ioff;
   v.M = M, v.tri_off = d_toff;
   v.verts = d_v, v.normals = d_n, v.vidx = d_vi, v.nidx = d_ni, v.matid = d_mat, v.mats = d_mats;
-  v.nodes = bb.nodes, v.leaves = bb.leaves, v.g = bb.g, v.args = b->args;
+  v.nodes = bb.nodes, v.wnodes = bb.wnodes, v.leaves = bb.leaves, v.g = bb.g, v.args = b->args;
   v.counter = bb.counters + 4;
   // per-mesh render arguments
   std::vector<RenderArgs> ha(M);
@@ -285,10 +287,12 @@ crt_status crt_batch_destroy(crt_batch* b) {
 
 crt_status crt_batch_set_tuning(crt_batch* b, const crt_batch_tuning* t) {
   if (!b || !t) return fail(CRT_INVALID_ARG, "null argument");
-  const bool ok = (t->block_size == 64 || t->block_size == 128 || t->block_size == 256) && t->tile_w > 0 &&
-                  t->tile_h > 0 && t->tile_w * t->tile_h == 32 && (t->stack == 0 || t->stack == 8 || t->stack == 16);
+  bool lanes_ok = false;
+  for (int s = 0; s < kLaneOptions; s++) lanes_ok = lanes_ok || t->lanes_per_pixel == kLanes[s];
+  const bool ok = (t->block_size == 64 || t->block_size == 128 || t->block_size == 256) && lanes_ok &&
+                  (t->stack == 0 || t->stack == 8 || t->stack == 16);
   if (!ok) return fail(CRT_INVALID_ARG, "unsupported tuning");
-  b->tuning.block = t->block_size, b->tuning.tw = t->tile_w, b->tuning.th = t->tile_h, b->tuning.stack = t->stack;
+  b->tuning.block = t->block_size, b->tuning.lanes = t->lanes_per_pixel, b->tuning.stack = t->stack;
   drop_graph(b);
   return CRT_OK;
 }
@@ -331,13 +335,13 @@ crt_status crt_batch_check(crt_batch* b, void* stream) {
   return CRT_OK;
 }
 
-// Times every supported tuning on the batch (build + render each, the graph
-// not used) and keeps the fastest; fills `chosen` if given.
+// Times the supported tunings on the batch (build once, then one render per
+// tuning after a warm-up render; lanes options that give every mesh the same
+// lanes per pixel as a smaller option are skipped) and keeps the fastest.
 crt_status crt_batch_autotune(crt_batch* b, crt_batch_tuning* chosen, void* stream) {
   if (!b) return fail(CRT_INVALID_ARG, "null batch");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int blocks[] = {64, 128, 256};
-  const int tiles[][2] = {{8, 4}, {4, 8}, {16, 2}, {32, 1}};
   const int stacks[] = {0, 8, 16};
   cudaEvent_t e0, e1;
   CRT_CUDA(cudaEventCreate(&e0), "event");
@@ -345,13 +349,17 @@ crt_status crt_batch_autotune(crt_batch* b, crt_batch_tuning* chosen, void* stre
   BatchTuning best = b->tuning;
   float best_ms = 1e30f;
   CRT_CUDA(launch_build_batch(b->b, st), "build");
-  for (int bs : blocks)
-    for (auto& tl : tiles)
+  CRT_CUDA(launch_render_batch(view_for(b, best), best, st), "render");  // warm-up
+  for (int li = 0; li < kLaneOptions; li++) {
+    bool same = li > 0;
+    for (int m = 0; m < b->M && same; m++)
+      same = lanes_per_pixel(b->views[m].spp, kLanes[li]) == lanes_per_pixel(b->views[m].spp, kLanes[li - 1]);
+    if (same) continue;
+    for (int bs : blocks)
       for (int sk : stacks) {
         BatchTuning t;
-        t.block = bs, t.tw = tl[0], t.th = tl[1], t.stack = sk;
+        t.block = bs, t.lanes = kLanes[li], t.stack = sk;
         const BatchView v = view_for(b, t);
-        CRT_CUDA(launch_render_batch(v, t, st), "render");  // warm-up
         CRT_CUDA(cudaEventRecord(e0, st), "event");
         CRT_CUDA(launch_render_batch(v, t, st), "render");
         CRT_CUDA(cudaEventRecord(e1, st), "event");
@@ -360,12 +368,13 @@ crt_status crt_batch_autotune(crt_batch* b, crt_batch_tuning* chosen, void* stre
         CRT_CUDA(cudaEventElapsedTime(&ms, e0, e1), "event");
         if (ms < best_ms) best_ms = ms, best = t;
       }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   b->tuning = best;
   drop_graph(b);
   if (chosen) {
-    chosen->block_size = best.block, chosen->tile_w = best.tw, chosen->tile_h = best.th, chosen->stack = best.stack;
+    chosen->block_size = best.block, chosen->lanes_per_pixel = best.lanes, chosen->stack = best.stack;
     chosen->render_ms = best_ms;
   }
   return CRT_OK;

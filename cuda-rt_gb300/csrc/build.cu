@@ -544,9 +544,31 @@ __device__ __forceinline__ void put_slot(BNode* P, bool left, const float lo[3],
   }
 }
 
+// The wide nodes (WNode) take the same boxes: child x (code xc) of binary
+// node p fills slot 2*side(p) + side(x) of the wide node of p's parent, and a
+// leaf child also fills its own slot of p's wide node (with the odd slot
+// marked empty).  Codes are rewritten with the boxes, so a refit alone keeps
+// the wide nodes complete.
+__device__ __forceinline__ void put_wide(WNode* W, int xc, bool x_left, int p, uint32_t wn, bool p_is_root,
+                                         const float lo[3], const float hi[3]) {
+  const float4 a = make_float4(lo[0], lo[1], lo[2], __int_as_float(xc));
+  const float4 b = make_float4(hi[0], hi[1], hi[2], 0.f);
+  if (xc < 0) {
+    WSlot* q = W[p].s + (x_left ? 0 : 2);
+    __stcg(&q[0].lo_code, a);
+    __stcg(&q[0].hi, b);
+    __stcg(&q[1].lo_code, make_float4(0.f, 0.f, 0.f, __int_as_float(kNoChild)));
+  }
+  if (!p_is_root) {
+    WSlot* q = W[wn & kParentMask].s + ((wn & kParentLeft) ? 0 : 2) + (x_left ? 0 : 1);
+    __stcg(&q->lo_code, a);
+    __stcg(&q->hi, b);
+  }
+}
+
 __global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__ V, const int* __restrict__ vidx,
                                                        const uint32_t* __restrict__ ids, int n, BNode* nodes,
-                                                       LeafTri* __restrict__ leaves,
+                                                       WNode* wnodes, LeafTri* __restrict__ leaves,
                                                        const uint32_t* __restrict__ parent, int* flags,
                                                        SceneGlobals* g) {
   __shared__ float s_box[kRefitBlock][2][6];  // children's boxes at each block-local node
@@ -574,6 +596,7 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__
       for (int q = 0; q < 3; q++) g->root_box[q] = lo[q], g->root_box[3 + q] = hi[q];
     } else {
       uint32_t w = __ldg(parent + (n - 1) + k);
+      int xc = ~k;  // code of the node that climbs (a leaf, then internal nodes)
       for (int level = 0;; level++) {
         const int p = (int)(w & kParentMask);
         if (level >= kStackSize || p >= n - 1) {  // only a corrupt tree gets here
@@ -584,6 +607,7 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__
         BNode* P = nodes + p;
         const bool is_left = (w & kParentLeft) != 0;
         put_slot(P, is_left, lo, hi);
+        put_wide(wnodes, xc, is_left, p, wn, p == 0, lo, hi);
         if (!(w & kParentSpans)) {  // both arrivals are threads of this block
           const int sl = p - k0;
           float* mine = s_box[sl][is_left ? 0 : 1];
@@ -608,6 +632,7 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__
           for (int q = 0; q < 3; q++) g->root_box[q] = lo[q], g->root_box[3 + q] = hi[q];
           break;
         }
+        xc = p;
         w = wn;
       }
     }
@@ -796,7 +821,8 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit_batch(const float* __rest
                                                              const uint32_t* __restrict__ ids,
                                                              const int* __restrict__ mesh_of,
                                                              const int* __restrict__ tri_off, int N, int NI,
-                                                             BNode* nodes, LeafTri* __restrict__ leaves,
+                                                             BNode* nodes, WNode* wnodes,
+                                                             LeafTri* __restrict__ leaves,
                                                              const uint32_t* __restrict__ parent, int* flags,
                                                              SceneGlobals* g) {
   __shared__ float s_box[kRefitBlock][2][6];
@@ -825,6 +851,7 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit_batch(const float* __rest
   }
   const int root = t0 - m;
   uint32_t w = __ldg(parent + NI + k);
+  int xc = ~(k - t0);  // codes are local to the mesh
   for (int level = 0;; level++) {
     const int p = (int)(w & kParentMask);
     if (level >= kStackSize || p < root || p >= root + n - 1) {  // only a corrupt tree gets here
@@ -835,6 +862,7 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit_batch(const float* __rest
     BNode* P = nodes + p;
     const bool is_left = (w & kParentLeft) != 0;
     put_slot(P, is_left, lo, hi);
+    put_wide(wnodes, xc, is_left, p, wn, p == root, lo, hi);
     if (!(w & kParentSpans)) {
       const int sl = p + m - k0;  // global leaf position of the node's index, within this block
       float* mine = s_box[sl][is_left ? 0 : 1];
@@ -858,6 +886,7 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit_batch(const float* __rest
       for (int q = 0; q < 3; q++) g[m].root_box[q] = lo[q], g[m].root_box[3 + q] = hi[q];
       return;
     }
+    xc = p - root;
     w = wn;
   }
 }
@@ -872,7 +901,7 @@ __global__ void k_refit_init(SceneGlobals* g) {
 void refit(const MeshBufs& m, const BuildBufs& b, cudaStream_t st) {
   const int n = m.ntri;
   k_refit<<<(n + kRefitBlock - 1) / kRefitBlock, kRefitBlock, 0, st>>>(m.verts, m.vidx, b.vals_b, n, b.nodes,
-                                                                        b.leaves, b.parent, b.flags, b.g);
+                                                                        b.wnodes, b.leaves, b.parent, b.flags, b.g);
 }
 }  // namespace
 
@@ -946,7 +975,8 @@ cudaError_t launch_build_batch(const BatchBufs& b, cudaStream_t st) {
   if (b.NI > 0)
     k_hierarchy_batch<<<(b.NI + 255) / 256, 256, 0, st>>>(b.keys_b, b.tri_off, M, b.NI, b.nodes, b.parent, b.flags);
   k_refit_batch<<<(N + kRefitBlock - 1) / kRefitBlock, kRefitBlock, 0, st>>>(
-      b.verts, b.vidx, b.vals_a, b.mesh_of, b.tri_off, N, b.NI, b.nodes, b.leaves, b.parent, b.flags, b.g);
+      b.verts, b.vidx, b.vals_a, b.mesh_of, b.tri_off, N, b.NI, b.nodes, b.wnodes, b.leaves, b.parent, b.flags,
+      b.g);
   return cudaGetLastError();
 }
 

@@ -7,7 +7,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/crt.h"
+#include "crt.h"
 #include "crt_internal.h"
 
 using namespace crt;
@@ -67,6 +67,7 @@ DScene dscene(const crt_scene* s) {
   d.matid = s->m.matid;
   d.mats = s->m.mats;
   d.nodes = s->b.nodes;
+  d.wnodes = s->b.wnodes;
   d.leaves = s->b.leaves;
   d.g = s->b.g;
   return d;
@@ -192,11 +193,12 @@ crt_status crt_scene_create(const crt_mesh_desc* d, void* stream, crt_scene** ou
   b.n = n;
   const int tiles = sort_tiles(n > 0 ? n : 1);
   const size_t nn = n > 0 ? 2 * (size_t)n - 1 : 0;
-  size_t off[10], total = 0;
-  const size_t sizes[10] = {4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n, 4 * 3 * (size_t)kRadix,
+  size_t off[11], total = 0;
+  const size_t sizes[11] = {4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n, 4 * 3 * (size_t)kRadix,
                             4 * 3 * (size_t)tiles * kRadix, 4 * nn, 4 * (size_t)(n > 1 ? n - 1 : 1),
-                            sizeof(BNode) * (size_t)(n > 1 ? n - 1 : 1), sizeof(LeafTri) * (size_t)(n > 0 ? n : 1)};
-  for (int i = 0; i < 10; i++) off[i] = total, total += align256(sizes[i]);
+                            sizeof(BNode) * (size_t)(n > 1 ? n - 1 : 1), sizeof(LeafTri) * (size_t)(n > 0 ? n : 1),
+                            sizeof(WNode) * (size_t)(n > 1 ? n - 1 : 1)};
+  for (int i = 0; i < 11; i++) off[i] = total, total += align256(sizes[i]);
   const size_t goff = total;
   total += align256(sizeof(SceneGlobals));
   ALLOC(s->block, total);
@@ -213,6 +215,7 @@ crt_status crt_scene_create(const crt_mesh_desc* d, void* stream, crt_scene** ou
   b.flags = reinterpret_cast<int*>(base + off[7]);
   b.nodes = reinterpret_cast<BNode*>(base + off[8]);
   b.leaves = reinterpret_cast<LeafTri*>(base + off[9]);
+  b.wnodes = reinterpret_cast<WNode*>(base + off[10]);
   b.g = reinterpret_cast<SceneGlobals*>(base + goff);
   if ((e = cudaMemsetAsync(b.g, 0, sizeof(SceneGlobals), st)) != cudaSuccess) return bail(e, "memset");
   if ((e = cudaMemsetAsync(b.flags, 0, sizes[7], st)) != cudaSuccess) return bail(e, "memset");
@@ -391,6 +394,7 @@ crt_status crt_render(crt_scene* s, const crt_camera* cam, const crt_light* ligh
   const size_t nsm = npx * (size_t)p->spp;
   RenderArgs a;
   a.W = p->width, a.H = p->height, a.spp = p->spp, a.row0 = row0, a.row1 = row1;
+  a.group = lanes_per_pixel(p->spp, kDefaultLanesPerPixel);
   // the constants of raytracer.cu:126-130, 144; tan on the host
   a.angle = std::tan(M_PI * 0.5 * cam->fov / 180.0f);
   a.aspect = double(p->width) / double(p->height);
@@ -468,6 +472,7 @@ crt_status crt_adjoint_lambert(crt_scene* s, const crt_camera* cam, const crt_li
   const size_t npx = (size_t)p->width * p->height;
   RenderArgs a;
   a.W = p->width, a.H = p->height, a.spp = p->spp, a.row0 = row0, a.row1 = row1;
+  a.group = lanes_per_pixel(p->spp, kDefaultLanesPerPixel);
   a.angle = std::tan(M_PI * 0.5 * cam->fov / 180.0f);
   a.aspect = double(p->width) / double(p->height);
   a.invW = 1.0 / double(p->width);

@@ -17,6 +17,9 @@ namespace crt {
 
 constexpr double kRayEps = 0.00000001;  // RAY_EPSILON, inc/common.h:2
 constexpr int kStackSize = 64;          // STACK_SIZE, kernels/bvh.cu:379
+// The four-wide traversal pushes up to three entries per wide level: trees of
+// height < 60 (see CRT_MAX_TRIANGLES) need at most 3 * 30 entries.
+constexpr int kWideStack = 96;
 
 // Material (inc/material.h:8-24): the fields shade() and the shadow test read.
 struct DMat {
@@ -32,6 +35,22 @@ struct __align__(16) BNode {
   float4 xy_r;  // right child lo.x, hi.x, lo.y, hi.y
   float4 z_lr;  // left lo.z, hi.z, right lo.z, hi.z
   int4 child;   // left code, right code, -, -
+};
+
+// Four-wide traversal node (128 bytes, one aligned 8 x 16-byte fetch): the
+// binary tree with every other level folded in.  Wide node i holds the
+// children of binary node i's children, in left-first order: slots 0-1 come
+// from the left child, 2-3 from the right; a leaf child takes its even slot
+// itself and leaves the odd one empty (code kNoChild).  Per slot: box lo in
+// xyz and the child's code (int bits) in w, box hi in xyz.  Codes as in
+// BNode; an internal code names both the binary node and its wide node.
+constexpr int kNoChild = (int)0x80000000;
+struct __align__(16) WSlot {
+  float4 lo_code;
+  float4 hi;
+};
+struct __align__(128) WNode {
+  WSlot s[4];
 };
 
 // The triangle of the leaf at sorted position k: its three vertices, the
@@ -66,6 +85,7 @@ struct DScene {
   const int* matid;
   const DMat* mats;
   const BNode* nodes;
+  const WNode* wnodes;
   const LeafTri* leaves;
   SceneGlobals* g;
 };
@@ -310,6 +330,7 @@ static __device__ __noinline__ TriHit tri_exact(double ox, double oy, double oz,
 struct HitRec {
   double t, alpha, beta;
   int id;
+  int pos;  // sorted position of the leaf (its rank in left-first DFS order)
 };
 
 // The pruning bound for the current best t, rounded up to float: best +
@@ -324,12 +345,16 @@ __device__ __forceinline__ float prune_bound(double best, float tau) {
 // left-first DFS order) and BVH_d::intersectAny (ANY = true: the first hit
 // in that order), kernels/bvh.cu:382-449.  The candidate set is the same as
 // the reference's: internal boxes pass a conservative filter (a superset of
-// the exact test, and a leaf's box passes exactly only if all its ancestors
-// pass exactly), each leaf's box and triangle are tested exactly, and leaves
-// are visited in the reference's order.  Returns 1 hit, 0 miss, -1 stack
-// overflow (impossible for trees of height < 64, see CRT_MAX_TRIANGLES).
-// STATS counts visited internal nodes and tested triangles (the traffic
-// model of the roofline figure); it changes nothing else.
+// the exact test that is monotone in the box, so a grandchild passing implies
+// its parent passes, and a leaf's box passes exactly only if all its
+// ancestors pass exactly), and each leaf's box and triangle are tested
+// exactly.  Leaves are sorted in left-first DFS order, so the reference's
+// closest hit is the candidate with the least (t, sorted position); the
+// closest-hit walk visits children nearest first and prunes, the any-hit walk
+// keeps the reference's left-first order.  Returns 1 hit, 0 miss, -1 stack
+// overflow (impossible for trees of height < 60, see CRT_MAX_TRIANGLES).
+// STATS counts visited wide nodes and tested triangles (the traffic model of
+// the roofline figure); it changes nothing else.
 struct TravStats {
   uint32_t nodes = 0, tris = 0;
 };
@@ -338,7 +363,7 @@ struct TravStats {
 // ring[i * blockDim.x]) with older entries spilled to local memory.
 template <int SHORT>
 struct TravStack {
-  int2 local[kStackSize];
+  int2 local[kWideStack];
   int2* ring;
   int sp = 0;
   __device__ __forceinline__ void push(int2 e) {
@@ -366,7 +391,16 @@ struct TravStack {
 // still due.  kPop marks "take the next node from the stack".
 constexpr int kLeafBoxDue = 1 << 30;
 constexpr int kLeafIndex = kLeafBoxDue - 1;
-constexpr int kPop = (int)0x80000000;
+constexpr int kPop = kNoChild;
+
+__device__ __forceinline__ void cswap(float& ta, int& ca, float& tb, int& cb) {
+  if (tb < ta) {
+    const float t = ta;
+    ta = tb, tb = t;
+    const int c = ca;
+    ca = cb, cb = c;
+  }
+}
 
 // Warp-synchronous traversal: all 32 lanes of the warp call it together
 // (`live` false: the lane has no ray and only takes part in the votes).
@@ -375,10 +409,8 @@ constexpr int kPop = (int)0x80000000;
 // or runs out of nodes; then the lanes holding a candidate run the exact
 // double tests together.  The double arithmetic is thus issued once per
 // round for the whole warp instead of once per lane.  A lane waits at its
-// candidate until it is tested, so candidates are tested one at a time in
-// left-first DFS order, each against the best hit so far, and the pruning
-// bound is current when the lane walks on: the result and the visited nodes
-// are those of the sequential traversal.
+// candidate until it is tested, so the pruning bound is current when it
+// walks on.
 template <bool ANY, bool STATS = false, int SHORT = 0>
 __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, const float rb[6], HitRec& h, bool live,
                                         TravStats* ts = nullptr, int2* ring = nullptr) {
@@ -421,32 +453,49 @@ __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, const fl
       }
       if (node >= 0) {
         if (STATS) ts->nodes++;
-        const float4* np = reinterpret_cast<const float4*>(S.nodes + node);
-        const float4 xl = __ldg(np + 0), xr = __ldg(np + 1), zz = __ldg(np + 2);
-        const int4 ch = __ldg(reinterpret_cast<const int4*>(np + 3));
-        float tl, tr;
-        bool hl = box_cons(r, xl.x, xl.y, xl.z, xl.w, zz.x, zz.y, tl);
-        bool hr = box_cons(r, xr.x, xr.y, xr.z, xr.w, zz.z, zz.w, tr);
-        if (!ANY) {
-          hl = hl && !(tl > pb);
-          hr = hr && !(tr > pb);
+        const float4* np = reinterpret_cast<const float4*>(S.wnodes + node);
+        float4 q[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) q[j] = __ldg(np + j);
+        int c[4];
+        float t[4];
+        int nhit = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          const float4 lo = q[2 * k], hi = q[2 * k + 1];
+          c[k] = __float_as_int(lo.w);
+          bool hk = c[k] != kNoChild && box_cons(r, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z, t[k]);
+          if (!ANY) hk = hk && !(t[k] > pb);
+          if (hk && c[k] < 0 && !box_sure(r, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z)) c[k] = ~(~c[k] | kLeafBoxDue);
+          if (!hk) c[k] = kNoChild;
+          if (ANY) t[k] = 0.f;  // pruning bounds are not used
+          else if (!hk) t[k] = __int_as_float(0x7f800000);
+          nhit += hk ? 1 : 0;
         }
-        int cl = ch.x, cr = ch.y;
-        if (hl && cl < 0 && !box_sure(r, xl.x, xl.y, xl.z, xl.w, zz.x, zz.y)) cl = ~(~cl | kLeafBoxDue);
-        if (hr && cr < 0 && !box_sure(r, xr.x, xr.y, xr.z, xr.w, zz.z, zz.w)) cr = ~(~cr | kLeafBoxDue);
-        if (hl) {
-          if (hr) {
-            if (stk.sp >= kStackSize) {
-              err = true;
-              run = false;
-              break;
-            }
-            stk.push(make_int2(cr, __float_as_int(tr)));
+        if (!ANY) {  // nearest first; misses (+inf) sort last
+          cswap(t[0], c[0], t[1], c[1]);
+          cswap(t[2], c[2], t[3], c[3]);
+          cswap(t[0], c[0], t[2], c[2]);
+          cswap(t[1], c[1], t[3], c[3]);
+          cswap(t[1], c[1], t[2], c[2]);
+        }
+        if (stk.sp + nhit > kWideStack) {
+          err = true;
+          run = false;
+          break;
+        }
+        // take the first hit slot now, stack the others so they pop in order
+        int next = kPop;
+        float tnext = 0.f;
+#pragma unroll
+        for (int k = 3; k >= 0; k--) {
+          if (c[k] != kNoChild) {
+            if (next != kPop) stk.push(make_int2(next, __float_as_int(tnext)));
+            next = c[k];
+            tnext = t[k];
           }
-          node = cl;
-        } else {
-          node = hr ? cr : kPop;
         }
+        node = next;
       } else {
         if (STATS) ts->tris++;
         const float4* lp = reinterpret_cast<const float4*>(S.leaves + (~node & kLeafIndex));
@@ -458,7 +507,8 @@ __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, const fl
     // double phase: the lanes holding a candidate, together
     if (__ballot_sync(0xffffffffu, pending) == 0u) break;
     if (pending) {
-      const float4* lp = reinterpret_cast<const float4*>(S.leaves + (~cand & kLeafIndex));
+      const int pos = ~cand & kLeafIndex;
+      const float4* lp = reinterpret_cast<const float4*>(S.leaves + pos);
       const float4 a = __ldg(lp), b = __ldg(lp + 1), c = __ldg(lp + 2);
       bool in_box = true;
       if (~cand & kLeafBoxDue) {  // the leaf's box, as the refit computes it from the same vertices
@@ -469,8 +519,8 @@ __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, const fl
       pending = false;
       if (in_box) {
         const TriHit th = tri_exact(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, a, b, c);
-        if (th.hit && (ANY || !have || th.t < h.t)) {
-          h.t = th.t, h.alpha = th.alpha, h.beta = th.beta, h.id = __float_as_int(a.w);
+        if (th.hit && (ANY || !have || th.t < h.t || (th.t == h.t && pos < h.pos))) {
+          h.t = th.t, h.alpha = th.alpha, h.beta = th.beta, h.id = __float_as_int(a.w), h.pos = pos;
           have = true;
           if (ANY) run = false;
           else pb = prune_bound(th.t, r.tau);

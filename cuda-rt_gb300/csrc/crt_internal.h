@@ -27,6 +27,7 @@ struct BuildBufs {
   uint32_t* parent = nullptr;  // 2n - 1: parent index (reference numbering) | left-child and spanning bits
   int* flags = nullptr;        // n - 1
   BNode* nodes = nullptr;      // n - 1
+  WNode* wnodes = nullptr;     // n - 1
   LeafTri* leaves = nullptr;   // n
   SceneGlobals* g = nullptr;
 };
@@ -55,6 +56,7 @@ struct BatchBufs {
   uint32_t* parent = nullptr;  // NI + N
   int* flags = nullptr;        // NI
   BNode* nodes = nullptr;      // NI (child codes local to each mesh)
+  WNode* wnodes = nullptr;     // NI
   LeafTri* leaves = nullptr;   // N
   SceneGlobals* g = nullptr;   // M
   unsigned* counters = nullptr;  // 4
@@ -75,8 +77,21 @@ cudaError_t launch_sort_pairs(const uint32_t* kin, const uint32_t* vin, uint32_t
                               int key_bits, void* scratch, int* err, cudaStream_t st);
 
 // trace.cu
+// The pixel kernels give each pixel G lanes (a power of two, at most 32 and
+// at most spp rounded down to a power of two), so a warp covers 32 / G
+// pixels, laid out as a tile_w(G) x tile_h(G) block.
+__host__ __device__ inline int lanes_per_pixel(int spp, int gmax) {
+  int g = 1;
+  while (2 * g <= spp && 2 * g <= gmax && g < 32) g *= 2;
+  return g;
+}
+__host__ __device__ inline int group_tile_w(int G) { return 32 / G >= 8 ? 8 : 32 / G; }
+__host__ __device__ inline int group_tile_h(int G) { return (32 / G) / group_tile_w(G); }
+constexpr int kDefaultLanesPerPixel = 4;
+
 struct RenderArgs {
   int W, H, spp, row0, row1;
+  int group;  // lanes per pixel (lanes_per_pixel)
   double angle, aspect, invW, invH, aperture, focal;
   double eye[3];
   double lpos[3], lcol[3], lradius, latt[3];
@@ -112,13 +127,14 @@ struct BatchView {
   const int* matid = nullptr;
   const DMat* mats = nullptr;
   const BNode* nodes = nullptr;
+  const WNode* wnodes = nullptr;
   const LeafTri* leaves = nullptr;
   SceneGlobals* g = nullptr;
   const RenderArgs* args = nullptr;  // M
   unsigned* counter = nullptr;
 };
 struct BatchTuning {
-  int block = 128, tw = 8, th = 4, stack = 0;
+  int block = 128, lanes = kDefaultLanesPerPixel, stack = 0;  // lanes: the most lanes a pixel may take
 };
 cudaError_t launch_render_batch(const BatchView& v, const BatchTuning& t, cudaStream_t st);
 cudaError_t launch_trace(const DScene& S, const double* rays, int64_t n, bool any, int* ids, double* t,

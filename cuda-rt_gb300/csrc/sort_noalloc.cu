@@ -18,7 +18,7 @@
 // them) race on it.
 #include <mutex>
 
-#include "../../include/crt.h"
+#include "crt.h"
 #include "crt_internal.h"
 
 namespace crt {

@@ -48,8 +48,6 @@ __global__ void __launch_bounds__(128) k_trace(DScene S, const double* __restric
   }
 }
 
-constexpr int kTileW = 8, kTileH = 4;
-
 enum PixelMode { kRender = 0, kRenderStats = 1, kAdjoint = 2 };
 
 // Warp-reduced atomic add of a double (light gradient: few addresses).
@@ -67,21 +65,34 @@ __device__ __forceinline__ void warp_add(double* dst, double v) {
 // position, albedo) for the Lambert and distance terms; visibility (which
 // triangle is hit, whether the shadow ray is blocked) is held fixed.
 //
-// All 32 lanes of the warp call it together, each with its own pixel (valid
-// false: a lane outside the image, which computes nothing and writes
-// nothing); sample k of every lane is traced by one warp-synchronous
-// traversal, so the double arithmetic of ray generation, exact tests and
-// shading is issued for the warp's lanes together.
+// All 32 lanes of the warp call it together.  G lanes (a power of two) share
+// one pixel and trace G of its samples at once, in waves of G samples; valid
+// false marks a pixel outside the image (its lanes compute and write
+// nothing).  The samples of a pixel share one mrand stream: sample k draws
+// two numbers for the lens and, when its primary ray hits, three for the
+// light, so where sample k starts in the stream depends on which earlier
+// samples hit.  Each lane guesses those hits (`pred`: the last wave's
+// majority), traces, and the lanes whose guess of an earlier sample proved
+// wrong trace again with the hits just observed; at least one more sample of
+// every group is settled per round, and the settled rays are exactly the
+// sequential ones.  Colours and depths are then summed in sample order.
 template <int MODE, int SHORT = 0>
-__device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int px, int py, bool valid, float rb[6],
-                                      float B, float D, TravStats& ts, D3& glight, int2* ring = nullptr) {
+__device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int px, int py, bool valid, int G,
+                                      unsigned& pred, float rb[6], float B, float D, TravStats& ts, D3& glight,
+                                      int2* ring = nullptr) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int g = lane & (G - 1);
+    const int base = lane - g;
+    const unsigned gmask = (G == 32) ? full : (((1u << G) - 1u) << base);
+    const unsigned below = gmask & ((1u << lane) - 1u);  // the lanes of my group before me
     const int gx = (A.W + 15) / 16;  // gridDim.x of the reference's 16x16 launch
     const D3 lpos = d3(A.lpos[0], A.lpos[1], A.lpos[2]);
     const int idx = (A.H - py - 1) * A.W + px;
     // getGlobalIdx_2D_2D (inc/indexing.h:4-9) of the pixel's thread in the
     // reference launch, seeded by initPNRG (kernels/mrand.cu:38-41).
     const uint32_t gid = (uint32_t)(((py / 16) * gx + px / 16) * 256 + (py % 16) * 16 + (px % 16));
-    uint32_t st = wang_hash(gid);
+    uint32_t wst = wang_hash(gid);  // stream position at the start of the wave
     const double xx = (2 * ((px + 0.5) * A.invW) - 1) * A.angle * A.aspect;
     const double yy = (1 - 2 * ((py + 0.5) * A.invH)) * A.angle;
     // the pinhole direction scaled to the focal plane: the same for every sample
@@ -89,33 +100,67 @@ __device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int 
     fdir = d3(fdir.x * A.focal, fdir.y * A.focal, fdir.z * A.focal);
     D3 acc = d3(0, 0, 0);
     double depth = 0.0;
-    D3 G = d3(0, 0, 0);
+    D3 G3 = d3(0, 0, 0);
     double Gd = 0.0;
     if (MODE == kAdjoint && valid) {
       const double inv = 1.0 / (double)A.spp;
-      G = d3(A.grad_rgb[3 * (int64_t)idx] * inv, A.grad_rgb[3 * (int64_t)idx + 1] * inv,
-             A.grad_rgb[3 * (int64_t)idx + 2] * inv);
+      G3 = d3(A.grad_rgb[3 * (int64_t)idx] * inv, A.grad_rgb[3 * (int64_t)idx + 1] * inv,
+              A.grad_rgb[3 * (int64_t)idx + 2] * inv);
       Gd = A.grad_depth ? A.grad_depth[idx] * inv : 0.0;
     }
-    for (int k = 0; k < A.spp; k++) {
+    const int waves = (A.spp + G - 1) / G;
+    for (int w = 0; w < waves; w++) {
+      const int k = w * G + g;
+      const bool act = valid && k < A.spp;
+      const unsigned actm = __ballot_sync(full, act);
       const int64_t si = (int64_t)idx * A.spp + k;
-      const double dofAngle = 2 * 3.14159265358979323846 * rand_double(st);
-      const double dofRadius = A.aperture * sqrt(rand_double(st)) / 2.0;
-      D3 org = d3(0.0, 0.0, 0.0);
-      if (dofRadius != 0.0) {  // a zero radius gives +-0 components, which no later operation can tell apart
-        org = d3(dofRadius * cos(dofAngle), dofRadius * sin(dofAngle), 0.0);
+      // primary rays, speculating on the hits of the group's earlier samples
+      unsigned guess = pred;
+      bool done = !act;
+      HitRec h;
+      int res = 0;
+      D3 org = d3(0, 0, 0), dir = d3(0, 0, 1);
+      uint32_t st = wst;
+      unsigned hits;
+      while (true) {
+        RayC rc;
+        if (!done) {
+          st = wst;
+          for (int t = 0; t < g; t++) {
+            xorshift32(st);
+            xorshift32(st);
+            if ((guess >> (base + t)) & 1u) {
+              xorshift32(st);
+              xorshift32(st);
+              xorshift32(st);
+            }
+          }
+          const double dofAngle = 2 * 3.14159265358979323846 * rand_double(st);
+          const double dofRadius = A.aperture * sqrt(rand_double(st)) / 2.0;
+          org = d3(0.0, 0.0, 0.0);
+          if (dofRadius != 0.0) {  // a zero radius gives +-0 components, which no later operation can tell apart
+            org = d3(dofRadius * cos(dofAngle), dofRadius * sin(dofAngle), 0.0);
+          }
+          dir = normalize_exact(fdir - org);
+          ray_setup(rc, org.x, org.y, org.z, dir.x, dir.y, dir.z, B, D);
+        } else {
+          ray_setup(rc, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0, B, D);
+        }
+        HitRec ht;
+        const int r = traverse<false, MODE == kRenderStats, SHORT>(S, rc, rb, ht, !done, &ts, ring);
+        if (!done) h = ht, res = r;
+        hits = __ballot_sync(full, act && res > 0);
+        // a lane is settled when every earlier sample of its group was guessed right
+        if (((guess ^ hits) & actm & below) == 0u) done = true;
+        guess = hits;
+        if (__all_sync(full, done)) break;
       }
-      const D3 dir = normalize_exact(fdir - org);
-      if (MODE != kAdjoint && A.rays && valid) {
+      if (res < 0) atomicOr(&S.g->err, kErrStack);
+      const bool hit = act && res > 0;
+      if (MODE != kAdjoint && A.rays && act) {
         double* rr = A.rays + 6 * si;
         rr[0] = org.x, rr[1] = org.y, rr[2] = org.z, rr[3] = dir.x, rr[4] = dir.y, rr[5] = dir.z;
       }
-      RayC rc;
-      ray_setup(rc, org.x, org.y, org.z, dir.x, dir.y, dir.z, B, D);
-      HitRec h;
-      const int res = traverse<false, MODE == kRenderStats, SHORT>(S, rc, rb, h, valid, &ts, ring);
-      if (res < 0) atomicOr(&S.g->err, kErrStack);
-      const bool hit = valid && res > 0;
       // traceRay up to the shadow ray (lanes with a hit)
       D3 q, N, V, L;
       double sN = 0.0, sL = 0.0, dist = 0.0, fall = 0.0, datt = 0.0;
@@ -149,6 +194,8 @@ __device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int 
       } else {
         ray_setup(sr, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0, B, D);
       }
+      // the next wave starts where the group's last sample ended
+      wst = __shfl_sync(full, st, base + G - 1);
       // Light::shadowAttenuation: any-hit from q towards the light
       HitRec s;
       const int sres = traverse<true, MODE == kRenderStats, SHORT>(S, sr, rb, s, hit, &ts, ring);
@@ -187,7 +234,7 @@ __device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int 
         I = I + d3(att.x * ds.x * A.lcol[0], att.y * ds.y * A.lcol[1], att.z * ds.z * A.lcol[2]);
         col = I;
         if (MODE == kAdjoint) {
-          const double Gc[3] = {G.x, G.y, G.z};
+          const double Gc[3] = {G3.x, G3.y, G3.z};
           const double sa[3] = {satt.x, satt.y, satt.z};
           const double dsv[3] = {ds.x, ds.y, ds.z};
           double S_lam = 0.0, gdatt = 0.0;
@@ -254,17 +301,28 @@ __device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int 
             atomicAdd(A.grad_verts + 3 * ic + 2, wc * w.z);
           }
         }
-        depth += h.t;
       }
-      acc = acc + col;
-      if (MODE != kAdjoint && valid) {
+      if (MODE != kAdjoint && act) {
         if (A.hit_id) A.hit_id[si] = hit ? h.id : -1;
         if (A.hit_t) A.hit_t[si] = hit ? h.t : 0.0;
         if (A.shadow) A.shadow[si] = sh;
         if (A.shadow_id) A.shadow_id[si] = shid;
       }
+      // sum in sample order (the reference adds the samples one by one)
+      for (int t = 0; t < G; t++) {
+        const double cx = __shfl_sync(full, col.x, base + t), cy = __shfl_sync(full, col.y, base + t),
+                     cz = __shfl_sync(full, col.z, base + t);
+        const double dt = __shfl_sync(full, hit ? h.t : 0.0, base + t);
+        if (w * G + t < A.spp) {
+          acc = acc + d3(cx, cy, cz);
+          if ((hits >> (base + t)) & 1u) depth += dt;
+        }
+      }
+      // guess for the next wave: the group's majority
+      const int nh = __popc(hits & gmask), na = __popc(actm & gmask);
+      pred = __ballot_sync(full, 2 * nh >= na);
     }
-    if (MODE == kAdjoint || !valid) return;
+    if (MODE == kAdjoint || !valid || g != 0) return;
     const double inv = (double)A.spp;
     acc = d3(acc.x / inv, acc.y / inv, acc.z / inv);
     if (A.rgbf) {
@@ -311,7 +369,7 @@ __device__ __forceinline__ void flush_stats(const RenderArgs& A, const TravStats
   }
 }
 
-// One scene: warps claim 8x4-pixel tiles of rows [row0, row1).
+// One scene: warps claim tiles of 32 / G pixels of rows [row0, row1).
 template <int MODE>
 __global__ void __launch_bounds__(128, 4) k_pixels(DScene S, RenderArgs A) {
   TravStats ts;
@@ -319,26 +377,30 @@ __global__ void __launch_bounds__(128, 4) k_pixels(DScene S, RenderArgs A) {
   float rb[6], B, D;
   scene_consts(S, rb, B, D);
   const int lane = threadIdx.x & 31;
-  const int tiles_x = (A.W + kTileW - 1) / kTileW;
-  const int tiles_y = (A.row1 - A.row0 + kTileH - 1) / kTileH;
+  const int G = A.group, tw = group_tile_w(G), th = group_tile_h(G);
+  const int tiles_x = (A.W + tw - 1) / tw;
+  const int tiles_y = (A.row1 - A.row0 + th - 1) / th;
   const int ntiles = tiles_x * tiles_y;
+  const int p = lane / G;  // this lane's pixel in the tile
+  unsigned pred = 0xffffffffu;
   while (true) {
     int tile = 0;
     if (lane == 0) tile = (int)atomicAdd(A.counter, 1u);
     tile = __shfl_sync(0xffffffffu, tile, 0);
     if (tile >= ntiles) break;
-    const int px = (tile % tiles_x) * kTileW + (lane % kTileW);
-    const int py = A.row0 + (tile / tiles_x) * kTileH + (lane / kTileW);
-    pixel<MODE>(S, A, px, py, px < A.W && py < A.row1, rb, B, D, ts, glight);
+    const int px = (tile % tiles_x) * tw + (p % tw);
+    const int py = A.row0 + (tile / tiles_x) * th + (p / tw);
+    pixel<MODE>(S, A, px, py, px < A.W && py < A.row1, G, pred, rb, B, D, ts, glight);
   }
   flush_stats<MODE>(A, ts, glight);
 }
 
 // Many scenes in one launch: work item i is (mesh, tile), with per-mesh tile
-// prefix sums item_off[M+1]; the warp's pixel tile is tw x th (tw * th = 32);
-// SHORT is the shared-memory part of the traversal stack (0: all local).
+// prefix sums item_off[M+1]; mesh m's pixels take lanes_per_pixel(spp,
+// gmax) lanes each; SHORT is the shared-memory part of the traversal stack
+// (0: all local).
 template <int SHORT>
-__global__ void __launch_bounds__(256, 2) k_pixels_batch(BatchView V, int tw, int th) {
+__global__ void __launch_bounds__(256, 2) k_pixels_batch(BatchView V, int gmax) {
   extern __shared__ int2 s_ring[];
   int2* ring = SHORT > 0 ? s_ring + threadIdx.x : nullptr;
   TravStats ts;
@@ -348,6 +410,8 @@ __global__ void __launch_bounds__(256, 2) k_pixels_batch(BatchView V, int tw, in
   DScene S;
   RenderArgs A;
   float rb[6], B = 0.f, D = 0.f;
+  unsigned pred = 0xffffffffu;
+  int G = 1, tw = 8, th = 4;
   while (true) {
     int item = 0;
     if (lane == 0) item = (int)atomicAdd(V.counter, 1u);
@@ -370,16 +434,19 @@ __global__ void __launch_bounds__(256, 2) k_pixels_batch(BatchView V, int tw, in
       S.root = n >= 2 ? 0 : ~0;
       S.verts = V.verts, S.normals = V.normals, S.vidx = V.vidx, S.nidx = V.nidx, S.matid = V.matid, S.mats = V.mats;
       S.nodes = V.nodes + (t0 - m);
+      S.wnodes = V.wnodes + (t0 - m);
       S.leaves = V.leaves + t0;
       S.g = V.g + m;
       A = V.args[m];
       scene_consts(S, rb, B, D);
+      G = lanes_per_pixel(A.spp, gmax), tw = group_tile_w(G), th = group_tile_h(G);
     }
     const int tile = item - __ldg(V.item_off + m);
     const int tiles_x = (A.W + tw - 1) / tw;
-    const int px = (tile % tiles_x) * tw + (lane % tw);
-    const int py = (tile / tiles_x) * th + (lane / tw);
-    pixel<kRender, SHORT>(S, A, px, py, px < A.W && py < A.H, rb, B, D, ts, glight, ring);
+    const int p = lane / G;
+    const int px = (tile % tiles_x) * tw + (p % tw);
+    const int py = (tile / tiles_x) * th + (p / tw);
+    pixel<kRender, SHORT>(S, A, px, py, px < A.W && py < A.H, G, pred, rb, B, D, ts, glight, ring);
   }
 }
 
@@ -402,11 +469,11 @@ cudaError_t launch_render(const DScene& S, const RenderArgs& a, cudaStream_t st)
 }
 
 template <int SHORT>
-static cudaError_t launch_batch_t(const BatchView& v, int block, int tw, int th, cudaStream_t st) {
+static cudaError_t launch_batch_t(const BatchView& v, int block, int gmax, cudaStream_t st) {
   const size_t smem = (size_t)SHORT * block * sizeof(int2);
   int bps = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_pixels_batch<SHORT>, block, smem);
-  k_pixels_batch<SHORT><<<num_sms() * (bps > 0 ? bps : 1), block, smem, st>>>(v, tw, th);
+  k_pixels_batch<SHORT><<<num_sms() * (bps > 0 ? bps : 1), block, smem, st>>>(v, gmax);
   return cudaGetLastError();
 }
 
@@ -414,11 +481,11 @@ cudaError_t launch_render_batch(const BatchView& v, const BatchTuning& t, cudaSt
   cudaMemsetAsync(v.counter, 0, sizeof(unsigned), st);
   switch (t.stack) {
     case 8:
-      return launch_batch_t<8>(v, t.block, t.tw, t.th, st);
+      return launch_batch_t<8>(v, t.block, t.lanes, st);
     case 16:
-      return launch_batch_t<16>(v, t.block, t.tw, t.th, st);
+      return launch_batch_t<16>(v, t.block, t.lanes, st);
     default:
-      return launch_batch_t<0>(v, t.block, t.tw, t.th, st);
+      return launch_batch_t<0>(v, t.block, t.lanes, st);
   }
 }
 

@@ -29,7 +29,7 @@ typedef enum crt_status {
   CRT_INVALID_ARG = 1,
   CRT_OOM = 2,
   CRT_CUDA_ERROR = 3,
-  CRT_STACK_OVERFLOW = 4, /* a traversal needed more than 64 stack entries */
+  CRT_STACK_OVERFLOW = 4, /* a traversal stack overflowed (impossible below CRT_MAX_TRIANGLES) */
   CRT_TIMEOUT = 5,        /* a bounded device-side wait gave up */
   CRT_NOT_BUILT = 6,      /* the scene has no BVH yet */
 } crt_status;
@@ -103,7 +103,7 @@ typedef struct crt_render_out {
   double* hit_t;     /* idx*spp + k: its t */
   int32_t* shadow;   /* idx*spp + k: 1 occluded, 0 lit, -1 primary miss */
   double* rays;      /* (idx*spp + k)*6: primary ray origin, direction */
-  uint64_t* traversal_stats; /* [2]: internal nodes visited, triangles tested (all
+  uint64_t* traversal_stats; /* [2]: four-wide nodes visited, leaf triangles tested (all
                                 rays of the call); non-NULL selects an instrumented kernel */
   double* rgb_f64;   /* idx*3: mean colour before clamping, in double */
   double* depth;     /* idx: mean over samples of the hit t (a miss counts 0) */
@@ -227,11 +227,12 @@ typedef struct crt_batch_view {
 } crt_batch_view;
 
 /* Launch shape of the batched pixel kernel: block_size in {64, 128, 256};
- * tile_w x tile_h = 32 pixels of one warp (8x4, 4x8, 16x2, 32x1); stack =
- * traversal-stack entries kept in shared memory per thread (0, 8, 16), the
- * rest of the 64 in local memory. */
+ * lanes_per_pixel in {1, 2, 4, 8, 16, 32}: the most lanes (rays traced at
+ * once) a pixel may take, capped by its samples per pixel, so a warp covers
+ * 32 / lanes pixels; stack = traversal-stack entries kept in shared memory
+ * per thread (0, 8, 16), the rest in local memory. */
 typedef struct crt_batch_tuning {
-  int32_t block_size, tile_w, tile_h, stack;
+  int32_t block_size, lanes_per_pixel, stack;
   float render_ms; /* written by crt_batch_autotune: the chosen shape's render time */
 } crt_batch_tuning;
 
@@ -247,8 +248,9 @@ crt_status crt_batch_destroy(crt_batch* batch);
  * the concatenated images; a host rgb8 synchronises `stream`. */
 crt_status crt_batch_run(crt_batch* batch, int32_t use_graph, uint8_t* rgb8, void* stream);
 crt_status crt_batch_set_tuning(crt_batch* batch, const crt_batch_tuning* tuning);
-/* Times the render under each of the 36 supported tunings (one warm-up and
- * one timed launch each, after one build) and keeps the fastest. */
+/* Times the render under each supported tuning (one launch each after a
+ * build and a warm-up render; lanes options that change no mesh's lanes per
+ * pixel are skipped) and keeps the fastest. */
 crt_status crt_batch_autotune(crt_batch* batch, crt_batch_tuning* chosen, void* stream);
 /* Mesh `mesh`'s build products in crt_bvh_export's layout (host or device
  * pointers; any may be NULL).  Synchronises `stream`. */

@@ -20,7 +20,7 @@ def _scenes():
     and two triangles; image sizes that are not multiples of any tile."""
     from crt import data
     sc = data.config3(count=10, lo=1_000, hi=20_000, width=48, height=40, spp=2, seed=5)
-    sizes = [(37, 23, 1), (64, 48, 2), (16, 16, 3), (33, 1, 2), (1, 31, 1)]
+    sizes = [(37, 23, 1), (64, 48, 2), (16, 16, 3), (33, 1, 5), (1, 31, 1), (20, 12, 16), (9, 7, 20)]
     out = []
     for i, s in enumerate(sc):
         w, h, spp = sizes[i % len(sizes)]
@@ -71,15 +71,15 @@ def test_batch_every_tuning_same_image(batch_case):
     crt, items, b = batch_case
     total = int(b.offsets[-1])
     ref = np.zeros((total, 3), np.uint8)
-    b.set_tuning(128, 8, 4, 0)
+    b.set_tuning(128, 1, 0)
     b.run(ref, graph=False)
     for bs in (64, 128, 256):
-        for tw, th in ((8, 4), (4, 8), (16, 2), (32, 1)):
+        for lanes in (1, 2, 4, 8, 16, 32):
             for stack in (0, 8, 16):
-                b.set_tuning(bs, tw, th, stack)
+                b.set_tuning(bs, lanes, stack)
                 out = np.zeros_like(ref)
                 b.run(out, graph=bool(stack & 8))
-                assert_equal(out, ref, f"tuning {bs} {tw}x{th} stack {stack}")
+                assert_equal(out, ref, f"tuning {bs} lanes {lanes} stack {stack}")
     b.check()
 
 
@@ -87,10 +87,11 @@ def test_batch_graph_replay_and_autotune(batch_case):
     crt, items, b = batch_case
     total = int(b.offsets[-1])
     first = np.zeros((total, 3), np.uint8)
-    b.set_tuning(128, 8, 4, 0)
+    b.set_tuning(128, 4, 0)
     b.run(first, graph=False)
     t = b.autotune()
-    assert t["block_size"] in (64, 128, 256) and t["tile_w"] * t["tile_h"] == 32 and t["stack"] in (0, 8, 16)
+    assert t["block_size"] in (64, 128, 256) and t["lanes_per_pixel"] in (1, 2, 4, 8, 16, 32)
+    assert t["stack"] in (0, 8, 16)
     assert t["render_ms"] > 0
     for _ in range(3):  # replays of one captured graph
         again = np.zeros_like(first)
