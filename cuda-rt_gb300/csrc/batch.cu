@@ -182,9 +182,9 @@ crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* v
   const size_t sz[] = {12 * (size_t)V, 12 * (size_t)Nn, 12 * (size_t)N, 12 * (size_t)N, 4 * (size_t)N,
                        sizeof(DMat) * (size_t)Mat, 4 * (size_t)N, 4 * (size_t)(M + 1), 4 * (size_t)kLaneOptions * (M + 1),
                        5 * 4 * (size_t)N, 4 * 4 * (size_t)kRadix, 4 * 4 * (size_t)tiles * kRadix,
-                       4 * (size_t)(NI + N), 4 * (size_t)(NI > 0 ? NI : 1), sizeof(BNode) * (size_t)(NI > 0 ? NI : 1),
+                       4 * (size_t)(NI + N), 4 * (size_t)(NI > 0 ? NI : 1), 0,
                        sizeof(LeafTri) * (size_t)N, sizeof(SceneGlobals) * (size_t)M, 64, b->image_bytes,
-                       sizeof(RenderArgs) * (size_t)M, sizeof(WNode) * (size_t)(NI > 0 ? NI : 1)};
+                       sizeof(RenderArgs) * (size_t)M, sizeof(WNode) * (size_t)(NI + M)};
   const int K = sizeof(sz) / sizeof(sz[0]);
   std::vector<size_t> off(K);
   size_t total = 0;
@@ -215,7 +215,6 @@ crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* v
   bb.status = (uint32_t*)at(11);
   bb.parent = (uint32_t*)at(12);
   bb.flags = (int*)at(13);
-  bb.nodes = (BNode*)at(14);
   bb.leaves = (LeafTri*)at(15);
   bb.g = (SceneGlobals*)at(16);
   bb.counters = (unsigned*)at(17);
@@ -227,7 +226,7 @@ crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* v
   b->d_item_off = d_ioff;
   v.M = M, v.tri_off = d_toff;
   v.verts = d_v, v.normals = d_n, v.vidx = d_vi, v.nidx = d_ni, v.matid = d_mat, v.mats = d_mats;
-  v.nodes = bb.nodes, v.wnodes = bb.wnodes, v.leaves = bb.leaves, v.g = bb.g, v.args = b->args;
+  v.wnodes = bb.wnodes, v.leaves = bb.leaves, v.g = bb.g, v.args = b->args;
   v.counter = bb.counters + 4;
   // per-mesh render arguments
   std::vector<RenderArgs> ha(M);
@@ -396,13 +395,15 @@ crt_status crt_batch_export(crt_batch* b, int32_t m, float* scene_box, int32_t* 
     return f;
   };
   std::vector<uint32_t> hk(n), hv(n), par_i(n > 1 ? n - 1 : 0), par_l(n);
-  std::vector<BNode> nd(n > 1 ? n - 1 : 0);
+  std::vector<WNode> wn(n > 1 ? n - 1 : 0);
+  WNode wroot;
   CRT_CUDA(cudaMemcpy(hk.data(), b->b.keys_b + t0, 4 * (size_t)n, cudaMemcpyDeviceToHost), "download");
   CRT_CUDA(cudaMemcpy(hv.data(), b->b.vals_a + t0, 4 * (size_t)n, cudaMemcpyDeviceToHost), "download");
   CRT_CUDA(cudaMemcpy(par_l.data(), b->b.parent + NI + t0, 4 * (size_t)n, cudaMemcpyDeviceToHost), "download");
   if (n > 1) {
     CRT_CUDA(cudaMemcpy(par_i.data(), b->b.parent + ib, 4 * (size_t)(n - 1), cudaMemcpyDeviceToHost), "download");
-    CRT_CUDA(cudaMemcpy(nd.data(), b->b.nodes + ib, sizeof(BNode) * (n - 1), cudaMemcpyDeviceToHost), "download");
+    CRT_CUDA(cudaMemcpy(wn.data(), b->b.wnodes + ib, sizeof(WNode) * (n - 1), cudaMemcpyDeviceToHost), "download");
+    CRT_CUDA(cudaMemcpy(&wroot, b->b.wnodes + NI + m, sizeof(WNode), cudaMemcpyDeviceToHost), "download");
   }
   const uint32_t mask = (1u << 30) - 1;
   std::vector<int> n3(3 * nn);
@@ -413,14 +414,23 @@ crt_status crt_batch_export(crt_batch* b, int32_t m, float* scene_box, int32_t* 
     n3[3 * ((n - 1) + k)] = n > 1 ? (int)(par_l[k] & mask) - ib : -1;
     n3[3 * ((n - 1) + k) + 1] = n3[3 * ((n - 1) + k) + 2] = (int)hv[k] - t0;
   }
+  // the children of internal node i sit in the wide node of its parent (the
+  // root's in the mesh's virtual node), slots 2*side(i) and 2*side(i) + 1
   for (int i = 0; i < n - 1; i++) {
-    const BNode& q = nd[i];
-    const int l = ref(q.child.x), r = ref(q.child.y);
-    n3[3 * i + 1] = l, n3[3 * i + 2] = r;
-    const float lb[6] = {q.xy_l.x, q.xy_l.z, q.z_lr.x, q.xy_l.y, q.xy_l.w, q.z_lr.y};
-    const float rbx[6] = {q.xy_r.x, q.xy_r.z, q.z_lr.z, q.xy_r.y, q.xy_r.w, q.z_lr.w};
-    std::memcpy(&nb[6 * (size_t)l], lb, sizeof(lb));
-    std::memcpy(&nb[6 * (size_t)r], rbx, sizeof(rbx));
+    const int pl = (int)(par_i[i] & mask) - ib;
+    if (i > 0 && (pl < 0 || pl >= n - 1)) return fail(CRT_CUDA_ERROR, "inconsistent tree");
+    const WNode& gw = i == 0 ? wroot : wn[pl];
+    const int s0 = (i == 0 || (par_i[i] >> 31)) ? 0 : 2;
+    for (int c = 0; c < 2; c++) {
+      const WSlot& q = gw.s[s0 + c];
+      int code;
+      std::memcpy(&code, &q.lo_code.w, 4);
+      const int r = ref(code);
+      if (code == kNoChild || r < 0 || (size_t)r >= nn) return fail(CRT_CUDA_ERROR, "inconsistent tree");
+      n3[3 * i + 1 + c] = r;
+      const float box[6] = {q.lo_code.x, q.lo_code.y, q.lo_code.z, q.hi.x, q.hi.y, q.hi.z};
+      std::memcpy(&nb[6 * (size_t)r], box, sizeof(box));
+    }
   }
   std::memcpy(&nb[0], g.root_box, 6 * sizeof(float));
   float box[6];

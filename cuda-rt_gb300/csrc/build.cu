@@ -481,9 +481,10 @@ constexpr int kRefitBlock = 512;
 constexpr uint32_t kParentLeft = 1u << 31, kParentSpans = 1u << 30, kParentMask = (1u << 30) - 1;
 
 // BuildHierarchy (kernels/bvh.cu:164-207) with FindSpan (bvh.cu:100-133) and
-// FindSplit (bvh.cu:134-162): one thread per internal node writes its child
-// codes, its children's parent words, and clears the node's refit flag.
-__global__ void __launch_bounds__(256) k_hierarchy(const uint32_t* __restrict__ codes, int n, BNode* __restrict__ nodes,
+// FindSplit (bvh.cu:134-162): one thread per internal node writes its
+// children's parent words and clears the node's refit flag (the child codes
+// reach the wide nodes through the refit, with the boxes).
+__global__ void __launch_bounds__(256) k_hierarchy(const uint32_t* __restrict__ codes, int n,
                                                    uint32_t* __restrict__ parent, int* __restrict__ flags) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n - 1) return;
@@ -514,7 +515,6 @@ __global__ void __launch_bounds__(256) k_hierarchy(const uint32_t* __restrict__ 
   const int split = left;
   const int c1 = (split == lo) ? ~split : split;
   const int c2 = (split + 1 == hi) ? ~(split + 1) : split + 1;
-  nodes[i].child = make_int4(c1, c2, 0, 0);
   const uint32_t spans = (lo / kRefitBlock != hi / kRefitBlock) ? kParentSpans : 0u;
   parent[c1 < 0 ? (n - 1) + split : split] = (uint32_t)i | kParentLeft | spans;
   parent[c2 < 0 ? (n - 1) + split + 1 : split + 1] = (uint32_t)i | spans;
@@ -524,32 +524,24 @@ __global__ void __launch_bounds__(256) k_hierarchy(const uint32_t* __restrict__ 
 // RefitBounds (kernels/bvh.cu:209-258): one climber per leaf; at each node the
 // first arrival stops and the second computes the union (bboxunion,
 // bvh.cu:63-69) and climbs on.  min/max are exact, so every schedule gives the
-// reference's boxes.  Boxes are stored in the parent's child slot (BNode).
+// reference's boxes.  Every box goes to the wide nodes (WNode): child x (code
+// xc) of binary node p fills slot 2*side(p) + side(x) of the wide node of p's
+// parent gp (for the root, the virtual node past the last internal one), and
+// a leaf child also fills its own slot of p's wide node, with the odd slot
+// marked empty.  Codes are rewritten with the boxes, so a refit alone keeps
+// the wide nodes complete, and the children of every node can be read back
+// from its parent's wide node (the export does).
 //
 // A block owns kRefitBlock consecutive sorted leaves.  A node whose leaf
 // range lies inside that span has both children's climbers in the block, so
 // its two arrivals meet in shared memory with block-scope ordering (most
 // nodes).  A node spanning several blocks uses the global flag with
-// release/acquire at gpu scope.  Global flags count arrivals; each refit adds
-// exactly two per spanning node, so the parity of the old value tells first
-// from second without clearing between refits.  Each climb step needs one
-// dependent load: the parent word (index, side, spanning bit).
-__device__ __forceinline__ void put_slot(BNode* P, bool left, const float lo[3], const float hi[3]) {
-  if (left) {
-    __stcg(&P->xy_l, make_float4(lo[0], hi[0], lo[1], hi[1]));
-    __stcg(reinterpret_cast<float2*>(&P->z_lr), make_float2(lo[2], hi[2]));
-  } else {
-    __stcg(&P->xy_r, make_float4(lo[0], hi[0], lo[1], hi[1]));
-    __stcg(reinterpret_cast<float2*>(&P->z_lr) + 1, make_float2(lo[2], hi[2]));
-  }
-}
-
-// The wide nodes (WNode) take the same boxes: child x (code xc) of binary
-// node p fills slot 2*side(p) + side(x) of the wide node of p's parent, and a
-// leaf child also fills its own slot of p's wide node (with the odd slot
-// marked empty).  Codes are rewritten with the boxes, so a refit alone keeps
-// the wide nodes complete.
-__device__ __forceinline__ void put_wide(WNode* W, int xc, bool x_left, int p, uint32_t wn, bool p_is_root,
+// release/acquire at gpu scope and reads its other child's box from the wide
+// node.  Global flags count arrivals; each refit adds exactly two per
+// spanning node, so the parity of the old value tells first from second
+// without clearing between refits.  Each climb step needs one dependent load:
+// the parent word (index, side, spanning bit).
+__device__ __forceinline__ void put_wide(WNode* W, int xc, bool x_left, int p, int gp, bool p_left,
                                          const float lo[3], const float hi[3]) {
   const float4 a = make_float4(lo[0], lo[1], lo[2], __int_as_float(xc));
   const float4 b = make_float4(hi[0], hi[1], hi[2], 0.f);
@@ -559,15 +551,22 @@ __device__ __forceinline__ void put_wide(WNode* W, int xc, bool x_left, int p, u
     __stcg(&q[0].hi, b);
     __stcg(&q[1].lo_code, make_float4(0.f, 0.f, 0.f, __int_as_float(kNoChild)));
   }
-  if (!p_is_root) {
-    WSlot* q = W[wn & kParentMask].s + ((wn & kParentLeft) ? 0 : 2) + (x_left ? 0 : 1);
-    __stcg(&q->lo_code, a);
-    __stcg(&q->hi, b);
-  }
+  WSlot* q = W[gp].s + (p_left ? 0 : 2) + (x_left ? 0 : 1);
+  __stcg(&q->lo_code, a);
+  __stcg(&q->hi, b);
+}
+
+// The box of the other child of p, from the wide node of p's parent.
+__device__ __forceinline__ void sibling_box(const WNode* W, int gp, bool p_left, bool x_left, float lo[3],
+                                            float hi[3]) {
+  const WSlot* q = W[gp].s + (p_left ? 0 : 2) + (x_left ? 1 : 0);
+  const float4 a = __ldcg(&q->lo_code), b = __ldcg(&q->hi);
+  lo[0] = fminf(lo[0], a.x), lo[1] = fminf(lo[1], a.y), lo[2] = fminf(lo[2], a.z);
+  hi[0] = fmaxf(hi[0], b.x), hi[1] = fmaxf(hi[1], b.y), hi[2] = fmaxf(hi[2], b.z);
 }
 
 __global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__ V, const int* __restrict__ vidx,
-                                                       const uint32_t* __restrict__ ids, int n, BNode* nodes,
+                                                       const uint32_t* __restrict__ ids, int n,
                                                        WNode* wnodes, LeafTri* __restrict__ leaves,
                                                        const uint32_t* __restrict__ parent, int* flags,
                                                        SceneGlobals* g) {
@@ -604,10 +603,14 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__
           break;
         }
         const uint32_t wn = (p == 0) ? 0u : __ldg(parent + p);  // next step's word, issued early
-        BNode* P = nodes + p;
         const bool is_left = (w & kParentLeft) != 0;
-        put_slot(P, is_left, lo, hi);
-        put_wide(wnodes, xc, is_left, p, wn, p == 0, lo, hi);
+        const int gp = (p == 0) ? n - 1 : (int)(wn & kParentMask);
+        const bool p_left = (p == 0) || (wn & kParentLeft) != 0;
+        if (gp >= n - 1 && p != 0) {  // only a corrupt tree gets here
+          atomicOr(&g->err, kErrStack);
+          break;
+        }
+        put_wide(wnodes, xc, is_left, p, gp, p_left, lo, hi);
         if (!(w & kParentSpans)) {  // both arrivals are threads of this block
           const int sl = p - k0;
           float* mine = s_box[sl][is_left ? 0 : 1];
@@ -622,10 +625,7 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__
         } else {
           // spanning node: release our slot, acquire the sibling's (gpu scope)
           if ((atomic_add_acq_rel(flags + p, 1) & 1) == 0) break;  // first arrival
-          const float4 xl = __ldcg(&P->xy_l), xr = __ldcg(&P->xy_r), zz = __ldcg(&P->z_lr);
-          lo[0] = fminf(xl.x, xr.x), hi[0] = fmaxf(xl.y, xr.y);
-          lo[1] = fminf(xl.z, xr.z), hi[1] = fmaxf(xl.w, xr.w);
-          lo[2] = fminf(zz.x, zz.z), hi[2] = fmaxf(zz.y, zz.w);
+          sibling_box(wnodes, gp, p_left, is_left, lo, hi);
         }
         if (p == 0) {
 #pragma unroll
@@ -649,9 +649,10 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__
 // ---------------------------------------------------------------- batched
 // The same build for many meshes at once (concatenated arrays; mesh m owns
 // triangles [tri_off[m], tri_off[m+1]) and internal nodes [int_off[m],
-// int_off[m+1]), int_off[m] = tri_off[m] - m).  Child codes in BNode are
-// local to the mesh, so each mesh's node and leaf ranges are a self-contained
-// tree for the traversal; parent words hold global internal indices.
+// int_off[m+1]), int_off[m] = tri_off[m] - m).  Child codes in the wide
+// nodes are local to the mesh, so each mesh's node and leaf ranges are a
+// self-contained tree for the traversal; parent words hold global internal
+// indices; mesh m's virtual wide node (its root's children) is NI + m.
 
 __global__ void k_batch_init(SceneGlobals* g, int M, uint32_t* hist, const int* __restrict__ tri_off,
                              unsigned* counters, int* err) {
@@ -768,7 +769,7 @@ __device__ __forceinline__ int mesh_of_internal(const int* __restrict__ tri_off,
 // BuildHierarchy per mesh (FindSpan/FindSplit on the mesh's sorted codes).
 __global__ void __launch_bounds__(256) k_hierarchy_batch(const uint32_t* __restrict__ codes_all,
                                                          const int* __restrict__ tri_off, int M, int NI,
-                                                         BNode* __restrict__ nodes, uint32_t* __restrict__ parent,
+                                                         uint32_t* __restrict__ parent,
                                                          int* __restrict__ flags) {
   const int gi = blockIdx.x * blockDim.x + threadIdx.x;
   if (gi >= NI) return;
@@ -806,7 +807,6 @@ __global__ void __launch_bounds__(256) k_hierarchy_batch(const uint32_t* __restr
   const int split = left;
   const int c1 = (split == lo) ? ~split : split;
   const int c2 = (split + 1 == hi) ? ~(split + 1) : split + 1;
-  nodes[gi].child = make_int4(c1, c2, 0, 0);
   const int ib = t0 - m;  // this mesh's first internal node
   const uint32_t spans = ((t0 + lo) / kRefitBlock != (t0 + hi) / kRefitBlock) ? kParentSpans : 0u;
   parent[c1 < 0 ? NI + t0 + split : ib + split] = (uint32_t)gi | kParentLeft | spans;
@@ -821,8 +821,7 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit_batch(const float* __rest
                                                              const uint32_t* __restrict__ ids,
                                                              const int* __restrict__ mesh_of,
                                                              const int* __restrict__ tri_off, int N, int NI,
-                                                             BNode* nodes, WNode* wnodes,
-                                                             LeafTri* __restrict__ leaves,
+                                                             WNode* wnodes, LeafTri* __restrict__ leaves,
                                                              const uint32_t* __restrict__ parent, int* flags,
                                                              SceneGlobals* g) {
   __shared__ float s_box[kRefitBlock][2][6];
@@ -859,10 +858,14 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit_batch(const float* __rest
       return;
     }
     const uint32_t wn = (p == root) ? 0u : __ldg(parent + p);
-    BNode* P = nodes + p;
     const bool is_left = (w & kParentLeft) != 0;
-    put_slot(P, is_left, lo, hi);
-    put_wide(wnodes, xc, is_left, p, wn, p == root, lo, hi);
+    const int gp = (p == root) ? NI + m : (int)(wn & kParentMask);
+    const bool p_left = (p == root) || (wn & kParentLeft) != 0;
+    if (p != root && (gp < root || gp >= root + n - 1)) {  // only a corrupt tree gets here
+      atomicOr(&g[m].err, kErrStack);
+      return;
+    }
+    put_wide(wnodes, xc, is_left, p, gp, p_left, lo, hi);
     if (!(w & kParentSpans)) {
       const int sl = p + m - k0;  // global leaf position of the node's index, within this block
       float* mine = s_box[sl][is_left ? 0 : 1];
@@ -876,10 +879,7 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit_batch(const float* __rest
       for (int q = 0; q < 3; q++) lo[q] = fminf(lo[q], o[q]), hi[q] = fmaxf(hi[q], o[3 + q]);
     } else {
       if ((atomic_add_acq_rel(flags + p, 1) & 1) == 0) return;
-      const float4 xl = __ldcg(&P->xy_l), xr = __ldcg(&P->xy_r), zz = __ldcg(&P->z_lr);
-      lo[0] = fminf(xl.x, xr.x), hi[0] = fmaxf(xl.y, xr.y);
-      lo[1] = fminf(xl.z, xr.z), hi[1] = fmaxf(xl.w, xr.w);
-      lo[2] = fminf(zz.x, zz.z), hi[2] = fmaxf(zz.y, zz.w);
+      sibling_box(wnodes, gp, p_left, is_left, lo, hi);
     }
     if (p == root) {
 #pragma unroll
@@ -900,8 +900,8 @@ __global__ void k_refit_init(SceneGlobals* g) {
 
 void refit(const MeshBufs& m, const BuildBufs& b, cudaStream_t st) {
   const int n = m.ntri;
-  k_refit<<<(n + kRefitBlock - 1) / kRefitBlock, kRefitBlock, 0, st>>>(m.verts, m.vidx, b.vals_b, n, b.nodes,
-                                                                        b.wnodes, b.leaves, b.parent, b.flags, b.g);
+  k_refit<<<(n + kRefitBlock - 1) / kRefitBlock, kRefitBlock, 0, st>>>(m.verts, m.vidx, b.vals_b, n, b.wnodes,
+                                                                        b.leaves, b.parent, b.flags, b.g);
 }
 }  // namespace
 
@@ -939,7 +939,7 @@ cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st)
     kin = ko;
     vin = vo;
   }
-  if (n >= 2) k_hierarchy<<<(n - 1 + 255) / 256, 256, 0, st>>>(b.keys_b, n, b.nodes, b.parent, b.flags);
+  if (n >= 2) k_hierarchy<<<(n - 1 + 255) / 256, 256, 0, st>>>(b.keys_b, n, b.parent, b.flags);
   refit(m, b, st);
   return cudaGetLastError();
 }
@@ -973,10 +973,9 @@ cudaError_t launch_build_batch(const BatchBufs& b, cudaStream_t st) {
                                               b.status + (size_t)3 * tiles * kRadix, b.counters + 3, b.err);
   k_gather_codes<<<ge, 256, 0, st>>>(b.vals_a, b.codes0, N, b.keys_b);
   if (b.NI > 0)
-    k_hierarchy_batch<<<(b.NI + 255) / 256, 256, 0, st>>>(b.keys_b, b.tri_off, M, b.NI, b.nodes, b.parent, b.flags);
+    k_hierarchy_batch<<<(b.NI + 255) / 256, 256, 0, st>>>(b.keys_b, b.tri_off, M, b.NI, b.parent, b.flags);
   k_refit_batch<<<(N + kRefitBlock - 1) / kRefitBlock, kRefitBlock, 0, st>>>(
-      b.verts, b.vidx, b.vals_a, b.mesh_of, b.tri_off, N, b.NI, b.nodes, b.wnodes, b.leaves, b.parent, b.flags,
-      b.g);
+      b.verts, b.vidx, b.vals_a, b.mesh_of, b.tri_off, N, b.NI, b.wnodes, b.leaves, b.parent, b.flags, b.g);
   return cudaGetLastError();
 }
 

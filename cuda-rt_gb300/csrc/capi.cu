@@ -66,7 +66,6 @@ DScene dscene(const crt_scene* s) {
   d.nidx = s->m.nidx;
   d.matid = s->m.matid;
   d.mats = s->m.mats;
-  d.nodes = s->b.nodes;
   d.wnodes = s->b.wnodes;
   d.leaves = s->b.leaves;
   d.g = s->b.g;
@@ -196,8 +195,7 @@ crt_status crt_scene_create(const crt_mesh_desc* d, void* stream, crt_scene** ou
   size_t off[11], total = 0;
   const size_t sizes[11] = {4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n, 4 * 3 * (size_t)kRadix,
                             4 * 3 * (size_t)tiles * kRadix, 4 * nn, 4 * (size_t)(n > 1 ? n - 1 : 1),
-                            sizeof(BNode) * (size_t)(n > 1 ? n - 1 : 1), sizeof(LeafTri) * (size_t)(n > 0 ? n : 1),
-                            sizeof(WNode) * (size_t)(n > 1 ? n - 1 : 1)};
+                            0, sizeof(LeafTri) * (size_t)(n > 0 ? n : 1), sizeof(WNode) * (size_t)(n > 0 ? n : 1)};
   for (int i = 0; i < 11; i++) off[i] = total, total += align256(sizes[i]);
   const size_t goff = total;
   total += align256(sizeof(SceneGlobals));
@@ -213,7 +211,6 @@ crt_status crt_scene_create(const crt_mesh_desc* d, void* stream, crt_scene** ou
   b.status = reinterpret_cast<uint32_t*>(base + off[5]);
   b.parent = reinterpret_cast<uint32_t*>(base + off[6]);
   b.flags = reinterpret_cast<int*>(base + off[7]);
-  b.nodes = reinterpret_cast<BNode*>(base + off[8]);
   b.leaves = reinterpret_cast<LeafTri*>(base + off[9]);
   b.wnodes = reinterpret_cast<WNode*>(base + off[10]);
   b.g = reinterpret_cast<SceneGlobals*>(base + goff);
@@ -310,13 +307,13 @@ crt_status crt_bvh_export(crt_scene* s, float* scene_box, int32_t* codes, uint32
   for (int k = 0; k < 3; k++) box[k] = ord2f_h(g.bmin[k]), box[3 + k] = ord2f_h(g.bmax[k]);
   std::vector<uint32_t> hk(n), hv(n);
   std::vector<int> parent(nn);
-  std::vector<BNode> nodes(n > 1 ? n - 1 : 0);
+  std::vector<WNode> wn(n > 1 ? n : 0);
   if (n > 0) {
     CRT_CUDA(cudaMemcpy(hk.data(), s->b.keys_b, 4 * (size_t)n, cudaMemcpyDeviceToHost), "download");
     CRT_CUDA(cudaMemcpy(hv.data(), s->b.vals_b, 4 * (size_t)n, cudaMemcpyDeviceToHost), "download");
     CRT_CUDA(cudaMemcpy(parent.data(), s->b.parent, 4 * nn, cudaMemcpyDeviceToHost), "download");
   }
-  if (n > 1) CRT_CUDA(cudaMemcpy(nodes.data(), s->b.nodes, sizeof(BNode) * (n - 1), cudaMemcpyDeviceToHost), "download");
+  if (n > 1) CRT_CUDA(cudaMemcpy(wn.data(), s->b.wnodes, sizeof(WNode) * (size_t)n, cudaMemcpyDeviceToHost), "download");
   std::vector<int> n3(3 * nn);
   std::vector<float> nb(6 * nn);
   auto ref = [n](int code) { return code >= 0 ? code : (n - 1) + ~code; };
@@ -325,15 +322,23 @@ crt_status crt_bvh_export(crt_scene* s, float* scene_box, int32_t* codes, uint32
     n3[3 * ((n - 1) + k) + 1] = (int)hv[k];
     n3[3 * ((n - 1) + k) + 2] = (int)hv[k];
   }
+  // the children of internal node i sit in the wide node of its parent (the
+  // root's in the virtual node n - 1), slots 2*side(i) and 2*side(i) + 1
   for (int i = 0; i < n - 1; i++) {
-    const BNode& b = nodes[i];
-    const int l = ref(b.child.x), r = ref(b.child.y);
-    n3[3 * i + 1] = l;
-    n3[3 * i + 2] = r;
-    const float lb[6] = {b.xy_l.x, b.xy_l.z, b.z_lr.x, b.xy_l.y, b.xy_l.w, b.z_lr.y};
-    const float rbx[6] = {b.xy_r.x, b.xy_r.z, b.z_lr.z, b.xy_r.y, b.xy_r.w, b.z_lr.w};
-    std::memcpy(&nb[6 * (size_t)l], lb, sizeof(lb));
-    std::memcpy(&nb[6 * (size_t)r], rbx, sizeof(rbx));
+    const uint32_t w = (uint32_t)parent[i];
+    const int gp = i == 0 ? n - 1 : (int)(w & ((1u << 30) - 1));
+    if (gp < 0 || gp >= n) return fail(CRT_CUDA_ERROR, "inconsistent tree");
+    const int s0 = (i == 0 || (w >> 31)) ? 0 : 2;
+    for (int c = 0; c < 2; c++) {
+      const WSlot& q = wn[gp].s[s0 + c];
+      int code;
+      std::memcpy(&code, &q.lo_code.w, 4);
+      const int r = ref(code);
+      if (code == kNoChild || r < 0 || (size_t)r >= nn) return fail(CRT_CUDA_ERROR, "inconsistent tree");
+      n3[3 * i + 1 + c] = r;
+      const float box[6] = {q.lo_code.x, q.lo_code.y, q.lo_code.z, q.hi.x, q.hi.y, q.hi.z};
+      std::memcpy(&nb[6 * (size_t)r], box, sizeof(box));
+    }
   }
   if (nn > 0) std::memcpy(&nb[0], g.root_box, 6 * sizeof(float));
   auto put = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {

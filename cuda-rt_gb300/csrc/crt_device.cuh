@@ -27,23 +27,18 @@ struct DMat {
   double shininess;
 };
 
-// Traversal node: the boxes of both children plus their codes (64 bytes, one
-// aligned 4 x 16-byte fetch).  Child code >= 0: internal node index in the
-// reference's numbering; child code < 0: leaf at sorted position ~code.
-struct __align__(16) BNode {
-  float4 xy_l;  // left  child lo.x, hi.x, lo.y, hi.y
-  float4 xy_r;  // right child lo.x, hi.x, lo.y, hi.y
-  float4 z_lr;  // left lo.z, hi.z, right lo.z, hi.z
-  int4 child;   // left code, right code, -, -
-};
-
 // Four-wide traversal node (128 bytes, one aligned 8 x 16-byte fetch): the
-// binary tree with every other level folded in.  Wide node i holds the
+// binary radix tree with every other level folded in.  Wide node i holds the
 // children of binary node i's children, in left-first order: slots 0-1 come
 // from the left child, 2-3 from the right; a leaf child takes its even slot
 // itself and leaves the odd one empty (code kNoChild).  Per slot: box lo in
-// xyz and the child's code (int bits) in w, box hi in xyz.  Codes as in
-// BNode; an internal code names both the binary node and its wide node.
+// xyz and the child's code (int bits) in w, box hi in xyz.  Child code >= 0:
+// internal node index in the reference's numbering (it names both the binary
+// node and its wide node); child code < 0: leaf at sorted position ~code.
+// The array has one entry more than there are internal nodes: that last,
+// virtual node holds the root's two children in slots 0 and 1 (the root
+// counts as its left child), so every node's children sit in the wide node
+// of its parent.
 constexpr int kNoChild = (int)0x80000000;
 struct __align__(16) WSlot {
   float4 lo_code;
@@ -84,7 +79,6 @@ struct DScene {
   const int* nidx;
   const int* matid;
   const DMat* mats;
-  const BNode* nodes;
   const WNode* wnodes;
   const LeafTri* leaves;
   SceneGlobals* g;

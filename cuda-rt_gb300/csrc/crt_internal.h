@@ -26,8 +26,7 @@ struct BuildBufs {
   uint32_t* status = nullptr;  // 3 * tiles * kRadix
   uint32_t* parent = nullptr;  // 2n - 1: parent index (reference numbering) | left-child and spanning bits
   int* flags = nullptr;        // n - 1
-  BNode* nodes = nullptr;      // n - 1
-  WNode* wnodes = nullptr;     // n - 1
+  WNode* wnodes = nullptr;     // n (the last one virtual: the root's children)
   LeafTri* leaves = nullptr;   // n
   SceneGlobals* g = nullptr;
 };
@@ -55,8 +54,7 @@ struct BatchBufs {
   uint32_t* status = nullptr;  // 4 * tiles * kRadix
   uint32_t* parent = nullptr;  // NI + N
   int* flags = nullptr;        // NI
-  BNode* nodes = nullptr;      // NI (child codes local to each mesh)
-  WNode* wnodes = nullptr;     // NI
+  WNode* wnodes = nullptr;     // NI + M (codes local to each mesh; NI + m: mesh m's virtual node)
   LeafTri* leaves = nullptr;   // N
   SceneGlobals* g = nullptr;   // M
   unsigned* counters = nullptr;  // 4
@@ -126,7 +124,6 @@ struct BatchView {
   const int* nidx = nullptr;
   const int* matid = nullptr;
   const DMat* mats = nullptr;
-  const BNode* nodes = nullptr;
   const WNode* wnodes = nullptr;
   const LeafTri* leaves = nullptr;
   SceneGlobals* g = nullptr;

@@ -370,8 +370,12 @@ __device__ __forceinline__ void flush_stats(const RenderArgs& A, const TravStats
 }
 
 // One scene: warps claim tiles of 32 / G pixels of rows [row0, row1).
+// SHORT: traversal-stack entries kept in shared memory per thread.
+constexpr int kPixelsShort = 0;
 template <int MODE>
 __global__ void __launch_bounds__(128, 4) k_pixels(DScene S, RenderArgs A) {
+  extern __shared__ int2 s_ring[];
+  int2* ring = kPixelsShort > 0 ? s_ring + threadIdx.x : nullptr;
   TravStats ts;
   D3 glight = d3(0, 0, 0);
   float rb[6], B, D;
@@ -390,7 +394,7 @@ __global__ void __launch_bounds__(128, 4) k_pixels(DScene S, RenderArgs A) {
     if (tile >= ntiles) break;
     const int px = (tile % tiles_x) * tw + (p % tw);
     const int py = A.row0 + (tile / tiles_x) * th + (p / tw);
-    pixel<MODE>(S, A, px, py, px < A.W && py < A.row1, G, pred, rb, B, D, ts, glight);
+    pixel<MODE, kPixelsShort>(S, A, px, py, px < A.W && py < A.row1, G, pred, rb, B, D, ts, glight, ring);
   }
   flush_stats<MODE>(A, ts, glight);
 }
@@ -433,7 +437,6 @@ __global__ void __launch_bounds__(256, 2) k_pixels_batch(BatchView V, int gmax) 
       S.ntri = n;
       S.root = n >= 2 ? 0 : ~0;
       S.verts = V.verts, S.normals = V.normals, S.vidx = V.vidx, S.nidx = V.nidx, S.matid = V.matid, S.mats = V.mats;
-      S.nodes = V.nodes + (t0 - m);
       S.wnodes = V.wnodes + (t0 - m);
       S.leaves = V.leaves + t0;
       S.g = V.g + m;
@@ -452,19 +455,22 @@ __global__ void __launch_bounds__(256, 2) k_pixels_batch(BatchView V, int gmax) 
 
 }  // namespace
 
+template <int MODE>
+static void launch_pixels(const DScene& S, const RenderArgs& a, cudaStream_t st) {
+  const size_t smem = (size_t)kPixelsShort * 128 * sizeof(int2);
+  int bps = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_pixels<MODE>, 128, smem);
+  k_pixels<MODE><<<num_sms() * (bps > 0 ? bps : 1), 128, smem, st>>>(S, a);
+}
+
 cudaError_t launch_render(const DScene& S, const RenderArgs& a, cudaStream_t st) {
   cudaMemsetAsync(a.counter, 0, sizeof(unsigned), st);
-  int bps = 0;
-  if (a.grad_rgb) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_pixels<kAdjoint>, 128, 0);
-    k_pixels<kAdjoint><<<num_sms() * (bps > 0 ? bps : 1), 128, 0, st>>>(S, a);
-  } else if (a.stats) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_pixels<kRenderStats>, 128, 0);
-    k_pixels<kRenderStats><<<num_sms() * (bps > 0 ? bps : 1), 128, 0, st>>>(S, a);
-  } else {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_pixels<kRender>, 128, 0);
-    k_pixels<kRender><<<num_sms() * (bps > 0 ? bps : 1), 128, 0, st>>>(S, a);
-  }
+  if (a.grad_rgb)
+    launch_pixels<kAdjoint>(S, a, st);
+  else if (a.stats)
+    launch_pixels<kRenderStats>(S, a, st);
+  else
+    launch_pixels<kRender>(S, a, st);
   return cudaGetLastError();
 }
 
