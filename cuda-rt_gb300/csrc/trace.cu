@@ -161,35 +161,21 @@ __device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int 
         double* rr = A.rays + 6 * si;
         rr[0] = org.x, rr[1] = org.y, rr[2] = org.z, rr[3] = dir.x, rr[4] = dir.y, rr[5] = dir.z;
       }
-      // traceRay up to the shadow ray (lanes with a hit)
-      D3 q, N, V, L;
-      double sN = 0.0, sL = 0.0, dist = 0.0, fall = 0.0, datt = 0.0;
-      bool tiny = false;
+      // traceRay up to the shadow ray (lanes with a hit): only what the
+      // shadow ray needs is computed before it, to keep little state live
+      // across the walk; the rest of the shading follows it
+      D3 q, L;
+      double sL = 0.0, dist = 0.0;
       RayC sr;
       if (hit) {
         q = org + (h.t * dir);
-        // smooth normal, bvh.cu:357-364 (hit_normal, kept apart for the adjoint)
-        const int na = S.nidx[3 * h.id], nb = S.nidx[3 * h.id + 1], nc = S.nidx[3 * h.id + 2];
-        const D3 nA = d3(S.normals[3 * na], S.normals[3 * na + 1], S.normals[3 * na + 2]);
-        const D3 nB = d3(S.normals[3 * nb], S.normals[3 * nb + 1], S.normals[3 * nb + 2]);
-        const D3 nC = d3(S.normals[3 * nc], S.normals[3 * nc + 1], S.normals[3 * nc + 2]);
-        const D3 Nr = (1.0 - (h.alpha + h.beta)) * nA + h.alpha * nB + h.beta * nC;
-        sN = 1.0 / (double)sqrtf(__double2float_rn(Nr.x * Nr.x + Nr.y * Nr.y + Nr.z * Nr.z));
-        N = d3(Nr.x * sN, Nr.y * sN, Nr.z * sN);
-        V = d3(A.eye[0], A.eye[1], A.eye[2]) - q;
-        V = normalize_exact(d3(-V.x, -V.y, -V.z));
         // Light::getDirection: three draws (x, y, z), times radius, minus 0.5
         const double r0 = rand_double(st), r1 = rand_double(st), r2 = rand_double(st);
         const D3 off = d3(r0 * A.lradius - 0.5, r1 * A.lradius - 0.5, r2 * A.lradius - 0.5);
         const D3 Lp = lpos + off - q;
         sL = 1.0 / (double)sqrtf(__double2float_rn(Lp.x * Lp.x + Lp.y * Lp.y + Lp.z * Lp.z));
         L = d3(Lp.x * sL, Lp.y * sL, Lp.z * sL);
-        // Light::distanceAttenuation
         dist = norm_exact(lpos - q);
-        fall = A.latt[0] + (A.latt[1] + A.latt[2] * dist) * dist;
-        tiny = fabs(fall) < kRayEps;
-        fall = tiny ? 1.0 : 1.0 / fall;
-        datt = fmin(1.0, fall);
         ray_setup(sr, q.x, q.y, q.z, L.x, L.y, L.z, B, D);
       } else {
         ray_setup(sr, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0, B, D);
@@ -200,6 +186,26 @@ __device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int 
       HitRec s;
       const int sres = traverse<true, MODE == kRenderStats, SHORT>(S, sr, rb, s, hit, &ts, ring);
       if (sres < 0) atomicOr(&S.g->err, kErrStack);
+      D3 N, V;
+      double sN = 0.0, fall = 0.0, datt = 0.0;
+      bool tiny = false;
+      if (hit) {
+        // smooth normal, bvh.cu:357-364 (hit_normal, kept apart for the adjoint)
+        const int na = S.nidx[3 * h.id], nb = S.nidx[3 * h.id + 1], nc = S.nidx[3 * h.id + 2];
+        const D3 nA = d3(S.normals[3 * na], S.normals[3 * na + 1], S.normals[3 * na + 2]);
+        const D3 nB = d3(S.normals[3 * nb], S.normals[3 * nb + 1], S.normals[3 * nb + 2]);
+        const D3 nC = d3(S.normals[3 * nc], S.normals[3 * nc + 1], S.normals[3 * nc + 2]);
+        const D3 Nr = (1.0 - (h.alpha + h.beta)) * nA + h.alpha * nB + h.beta * nC;
+        sN = 1.0 / (double)sqrtf(__double2float_rn(Nr.x * Nr.x + Nr.y * Nr.y + Nr.z * Nr.z));
+        N = d3(Nr.x * sN, Nr.y * sN, Nr.z * sN);
+        V = d3(A.eye[0], A.eye[1], A.eye[2]) - q;
+        V = normalize_exact(d3(-V.x, -V.y, -V.z));
+        // Light::distanceAttenuation
+        fall = A.latt[0] + (A.latt[1] + A.latt[2] * dist) * dist;
+        tiny = fabs(fall) < kRayEps;
+        fall = tiny ? 1.0 : 1.0 / fall;
+        datt = fmin(1.0, fall);
+      }
       D3 col = d3(0.9, 0.9, 0.9);
       int sh = -1, shid = -1;
       if (hit) {
@@ -412,7 +418,7 @@ __global__ void __launch_bounds__(256, 2) k_pixels_batch(BatchView V, int gmax) 
   const int lane = threadIdx.x & 31;
   int cur = -1;
   DScene S;
-  RenderArgs A;
+  const RenderArgs* Ap = V.args;  // the mesh's arguments, read through L1 rather than held in registers
   float rb[6], B = 0.f, D = 0.f;
   unsigned pred = 0xffffffffu;
   int G = 1, tw = 8, th = 4;
@@ -440,16 +446,17 @@ __global__ void __launch_bounds__(256, 2) k_pixels_batch(BatchView V, int gmax) 
       S.wnodes = V.wnodes + (t0 - m);
       S.leaves = V.leaves + t0;
       S.g = V.g + m;
-      A = V.args[m];
+      Ap = V.args + m;
       scene_consts(S, rb, B, D);
-      G = lanes_per_pixel(A.spp, gmax), tw = group_tile_w(G), th = group_tile_h(G);
+      G = lanes_per_pixel(Ap->spp, gmax), tw = group_tile_w(G), th = group_tile_h(G);
     }
     const int tile = item - __ldg(V.item_off + m);
-    const int tiles_x = (A.W + tw - 1) / tw;
+    const int W = Ap->W, H = Ap->H;
+    const int tiles_x = (W + tw - 1) / tw;
     const int p = lane / G;
     const int px = (tile % tiles_x) * tw + (p % tw);
     const int py = (tile / tiles_x) * th + (p / tw);
-    pixel<kRender, SHORT>(S, A, px, py, px < A.W && py < A.H, G, pred, rb, B, D, ts, glight, ring);
+    pixel<kRender, SHORT>(S, *Ap, px, py, px < W && py < H, G, pred, rb, B, D, ts, glight, ring);
   }
 }
 
