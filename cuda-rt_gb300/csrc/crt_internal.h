@@ -77,13 +77,14 @@ cudaError_t launch_sort_pairs(const uint32_t* kin, const uint32_t* vin, uint32_t
 // trace.cu
 // The pixel kernels give each pixel G lanes (a power of two, at most 32 and
 // at most spp rounded down to a power of two), so a warp covers 32 / G
-// pixels, laid out as a tile_w(G) x tile_h(G) block.
+// pixels, laid out as a tile_w(G) x tile_h(G) block (8x4, 8x2, 4x2, 2x2,
+// 2x1, 1x1: the most compact, for coherent rays).
 __host__ __device__ inline int lanes_per_pixel(int spp, int gmax) {
   int g = 1;
   while (2 * g <= spp && 2 * g <= gmax && g < 32) g *= 2;
   return g;
 }
-__host__ __device__ inline int group_tile_w(int G) { return 32 / G >= 8 ? 8 : 32 / G; }
+__host__ __device__ inline int group_tile_w(int G) { return 32 / G >= 16 ? 8 : (32 / G >= 4 ? 32 / G / 2 : 32 / G); }
 __host__ __device__ inline int group_tile_h(int G) { return (32 / G) / group_tile_w(G); }
 constexpr int kDefaultLanesPerPixel = 4;
 
