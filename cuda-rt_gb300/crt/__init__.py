@@ -20,7 +20,7 @@ import numpy as np
 from . import data  # noqa: F401
 from .build import LIB as LIB_PATH
 
-__all__ = ["CrtError", "Scene", "Batch", "lib", "sort_pairs", "sort_pairs_noalloc", "morton", "STATUS", "render_args"]
+__all__ = ["CrtError", "Scene", "Batch", "load_obj_native", "write_bmp", "lib", "sort_pairs", "sort_pairs_noalloc", "morton", "STATUS", "render_args"]
 
 STATUS = {0: "CRT_OK", 1: "CRT_INVALID_ARG", 2: "CRT_OOM", 3: "CRT_CUDA_ERROR", 4: "CRT_STACK_OVERFLOW",
           5: "CRT_TIMEOUT", 6: "CRT_NOT_BUILT"}
@@ -108,6 +108,10 @@ def lib():
             "crt_batch_autotune": [vp, vp, vp],
             "crt_batch_export": [vp, i32, vp, vp, vp, vp, vp, vp],
             "crt_batch_check": [vp, vp],
+            "crt_obj_load": [C.c_char_p, C.c_char_p, vp],
+            "crt_obj_mesh": [vp, vp],
+            "crt_obj_free": [vp],
+            "crt_write_bmp": [C.c_char_p, i32, i32, vp],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -346,6 +350,38 @@ class Batch:
         _check(lib().crt_batch_export(self.h, m, *[_addr(out[k]) for k in ("scene_box", "codes", "ids", "nodes",
                                                                             "node_boxes")], _stream(stream)))
         return out
+
+
+def load_obj_native(path, mtl_dir=None):
+    """crt_obj_load: the library's OBJ/MTL reader (host only), as a data.Mesh."""
+    from .data import Mesh
+    h = C.c_void_p()
+    _check(lib().crt_obj_load(os.fsencode(path), None if mtl_dir is None else os.fsencode(mtl_dir), C.byref(h)))
+    try:
+        d = _MeshDesc()
+        _check(lib().crt_obj_mesh(h, C.byref(d)))
+
+        def arr(ptr, n, ct, dt, shape):
+            if n == 0:
+                return np.zeros(shape, dt)
+            return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ct)), (n,)).astype(dt).reshape(shape)
+
+        n, nv, nn, nm = d.num_triangles, d.num_vertices, d.num_normals, d.num_materials
+        return Mesh(arr(d.vertices, 3 * nv, C.c_float, np.float32, (nv, 3)),
+                    arr(d.vertex_indices, 3 * n, C.c_int32, np.int32, (n, 3)),
+                    arr(d.normals, 3 * nn, C.c_float, np.float32, (nn, 3)),
+                    arr(d.normal_indices, 3 * n, C.c_int32, np.int32, (n, 3)),
+                    arr(d.material_ids, n, C.c_int32, np.int32, (n,)),
+                    arr(d.materials, 16 * nm, C.c_double, np.float64, (nm, 16)))
+    finally:
+        lib().crt_obj_free(h)
+
+
+def write_bmp(path, rgb8, width, height):
+    """crt_write_bmp: a 24-bit BMP of an rgb8 image in the library's bottom-up order."""
+    a = np.ascontiguousarray(rgb8, np.uint8)
+    assert a.size == 3 * width * height
+    _check(lib().crt_write_bmp(os.fsencode(path), width, height, a.ctypes.data))
 
 
 def render_args(camera, light, width, height, spp, rows=None):

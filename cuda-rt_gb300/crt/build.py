@@ -19,6 +19,8 @@ CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libcrt.so")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
+CLI_DIR = os.path.join(PKG, "cli")
+CLI = os.path.join(LIBDIR, "crt_raytracer")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE]
@@ -46,6 +48,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
         glob.glob(os.path.join(INCLUDE, "*.h"))
     srcs = sources()
     if not force and not _stale(LIB, srcs + headers + [__file__]):
+        build_cli()
         return LIB
     objs, procs = [], []
     for src in srcs:
@@ -68,7 +71,18 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     tmp = LIB + ".tmp"
     subprocess.check_call([nvcc(), *ARCH, "-shared", "-o", tmp, *objs])
     os.replace(tmp, LIB)
+    build_cli()
     return LIB
+
+
+def build_cli() -> str:
+    """The drop-in command-line renderer (cli/crt_raytracer.cpp), linked
+    against libcrt.so next to it."""
+    src = os.path.join(CLI_DIR, "crt_raytracer.cpp")
+    if _stale(CLI, [src, LIB, os.path.join(INCLUDE, "crt.h")]):
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-I", INCLUDE, src, "-L", LIBDIR, "-lcrt",
+                               "-Wl,-rpath,$ORIGIN", "-o", CLI])
+    return CLI
 
 
 if __name__ == "__main__":

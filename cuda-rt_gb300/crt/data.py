@@ -350,7 +350,9 @@ def config4(nu=100, width=512, height=512, spp=4, perturbed=False) -> Scene:
 def load_obj(path: str) -> Mesh:
     """Minimal Wavefront OBJ/MTL reader with tinyobjloader's conventions as the
     reference calls it (src/scene.cpp:6-58): polygons fan-triangulated, per-face
-    material ids, Ka/Kd/Ks/Kt(Tf)/Ke/Ns from the MTL file next to the OBJ."""
+    material ids, Ka/Kd/Ks/Kt(Tf)/Ke/Ns from the MTL file next to the OBJ
+    (colours default to 0, shininess to 1).  The C ABI's crt_obj_load reads the
+    same files to the same arrays."""
     import os
     verts, normals, vidx, nidx, matid = [], [], [], [], []
     mat_names, mats = {}, []
@@ -368,6 +370,7 @@ def load_obj(path: str) -> Mesh:
                     continue
                 if t[0] == "newmtl":
                     m = np.zeros(16, np.float64)
+                    m[15] = 1.0  # tinyobjloader's default shininess
                     mat_names[t[1]] = len(mats)
                     mats.append(m)
                 elif m is not None:

@@ -1,0 +1,262 @@
+// obj.cu -- host-side scene input and image output for the drop-in CLI:
+// a Wavefront OBJ/MTL reader with the conventions of the reference's loader
+// (Scene_h::LoadObj, src/scene.cpp:6-58, over its vendored tinyobjloader)
+// and the reference's 24-bit BMP writer (writeBMP, src/bitmap.cpp:99-154).
+// Host code only; no CUDA calls.
+//
+// OBJ: "v x y z", "vn x y z", "f" with v, v/t, v//n or v/t/n corners
+// (1-based or negative indices), polygons fan-triangulated (0, k, k+1),
+// "mtllib" (read from mtl_dir, or the OBJ's directory), "usemtl" (unknown
+// or absent names give material 0).  Coordinates are rounded to FP32, the
+// precision of crt_mesh_desc.  MTL: newmtl, Ka, Kd, Ks, Kt/Tf, Ke, Ns
+// (tinyobjloader's defaults: colours 0, shininess 1).  A missing MTL file
+// is skipped, as tinyobjloader warns and goes on; a mesh without materials
+// gets one Lambert material (kd 0.8).  Every face corner must name a normal:
+// the reference reads normals[-1] otherwise, so such files are rejected.
+#include <cerrno>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "crt.h"
+
+namespace crt {
+void set_last_error(const char* msg);
+}
+
+struct crt_obj {
+  std::vector<float> v, n;
+  std::vector<int32_t> vi, ni, mid;
+  std::vector<crt_material> mats;
+};
+
+namespace {
+
+crt_status fail(const std::string& m) {
+  crt::set_last_error(m.c_str());
+  return CRT_INVALID_ARG;
+}
+
+bool parse_double(const std::string& s, double& out) {
+  const char* b = s.c_str();
+  char* e = nullptr;
+  errno = 0;
+  out = std::strtod(b, &e);
+  return e != b && *e == '\0';
+}
+
+bool parse3(const std::vector<std::string>& t, double out[3]) {
+  if (t.size() < 4) return false;
+  for (int k = 0; k < 3; k++)
+    if (!parse_double(t[1 + k], out[k])) return false;
+  return true;
+}
+
+std::vector<std::string> split_ws(const std::string& line) {
+  std::vector<std::string> t;
+  std::istringstream is(line);
+  std::string w;
+  while (is >> w) t.push_back(w);
+  return t;
+}
+
+std::string dir_of(const std::string& path) {
+  const size_t k = path.find_last_of('/');
+  return k == std::string::npos ? std::string() : path.substr(0, k + 1);
+}
+
+void read_mtl(const std::string& file, std::map<std::string, int>& names, std::vector<crt_material>& mats) {
+  std::ifstream f(file);
+  if (!f) return;  // tinyobjloader warns and goes on
+  std::string line;
+  crt_material* m = nullptr;
+  while (std::getline(f, line)) {
+    const std::vector<std::string> t = split_ws(line);
+    if (t.empty()) continue;
+    if (t[0] == "newmtl" && t.size() >= 2) {
+      crt_material z;
+      std::memset(&z, 0, sizeof(z));
+      z.shininess = 1.0;
+      names[t[1]] = (int)mats.size();
+      mats.push_back(z);
+      m = &mats.back();
+      continue;
+    }
+    if (!m) continue;
+    double x[3];
+    double* dst = nullptr;
+    if (t[0] == "Ka") dst = m->ka;
+    else if (t[0] == "Kd") dst = m->kd;
+    else if (t[0] == "Ks") dst = m->ks;
+    else if (t[0] == "Kt" || t[0] == "Tf") dst = m->kt;
+    else if (t[0] == "Ke") dst = m->ke;
+    if (dst && parse3(t, x)) {
+      for (int k = 0; k < 3; k++) dst[k] = x[k];
+    } else if (t[0] == "Ns" && t.size() >= 2) {
+      double s;
+      if (parse_double(t[1], s)) m->shininess = s;
+    }
+  }
+}
+
+// One face corner: "v", "v/t", "v//n" or "v/t/n"; indices resolved to 0-based.
+bool corner(const std::string& c, size_t nv, size_t nn, int& vi, int& ni) {
+  const size_t s1 = c.find('/');
+  const std::string vs = c.substr(0, s1);
+  std::string ns;
+  if (s1 != std::string::npos) {
+    const size_t s2 = c.find('/', s1 + 1);
+    if (s2 != std::string::npos) ns = c.substr(s2 + 1);
+  }
+  char* e = nullptr;
+  const long v = std::strtol(vs.c_str(), &e, 10);
+  if (vs.empty() || *e != '\0' || v == 0) return false;
+  vi = v > 0 ? (int)(v - 1) : (int)((long)nv + v);
+  ni = -1;
+  if (!ns.empty()) {
+    const long n = std::strtol(ns.c_str(), &e, 10);
+    if (*e != '\0' || n == 0) return false;
+    ni = n > 0 ? (int)(n - 1) : (int)((long)nn + n);
+  }
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+crt_status crt_obj_load(const char* obj_path, const char* mtl_dir, crt_obj** out) {
+  if (!obj_path || !out) return fail("null argument");
+  *out = nullptr;
+  std::ifstream f(obj_path);
+  if (!f) return fail(std::string("cannot open ") + obj_path);
+  const std::string base = mtl_dir ? std::string(mtl_dir) : dir_of(obj_path);
+  crt_obj* o = new crt_obj;
+  std::map<std::string, int> names;
+  int cur = -1;
+  std::string line;
+  size_t lineno = 0;
+  while (std::getline(f, line)) {
+    lineno++;
+    const std::vector<std::string> t = split_ws(line);
+    if (t.empty() || t[0][0] == '#') continue;
+    double x[3];
+    if (t[0] == "v" || t[0] == "vn") {
+      if (!parse3(t, x)) {
+        delete o;
+        return fail("bad vertex at line " + std::to_string(lineno));
+      }
+      std::vector<float>& dst = t[0] == "v" ? o->v : o->n;
+      for (int k = 0; k < 3; k++) dst.push_back((float)x[k]);
+    } else if (t[0] == "mtllib" && t.size() >= 2) {
+      std::string p = base;
+      if (!p.empty() && p.back() != '/') p += '/';
+      read_mtl(p + t[1], names, o->mats);
+    } else if (t[0] == "usemtl") {
+      const auto it = t.size() >= 2 ? names.find(t[1]) : names.end();
+      cur = it == names.end() ? -1 : it->second;
+    } else if (t[0] == "f") {
+      std::vector<int> cv, cn;
+      for (size_t k = 1; k < t.size(); k++) {
+        int vi, ni;
+        if (!corner(t[k], o->v.size() / 3, o->n.size() / 3, vi, ni)) {
+          delete o;
+          return fail("bad face corner at line " + std::to_string(lineno));
+        }
+        if (ni < 0) {
+          delete o;
+          return fail("face without a normal index at line " + std::to_string(lineno) +
+                      " (vn normals are required)");
+        }
+        cv.push_back(vi);
+        cn.push_back(ni);
+      }
+      for (size_t k = 1; k + 1 < cv.size(); k++) {
+        const size_t c3[3] = {0, k, k + 1};
+        for (size_t j : c3) o->vi.push_back(cv[j]), o->ni.push_back(cn[j]);
+        o->mid.push_back(cur);
+      }
+    }
+  }
+  if (o->mats.empty()) {
+    crt_material z;
+    std::memset(&z, 0, sizeof(z));
+    z.kd[0] = z.kd[1] = z.kd[2] = 0.8;
+    o->mats.push_back(z);
+  }
+  for (int32_t& m : o->mid)
+    if (m < 0) m = 0;
+  const int64_t nv = (int64_t)o->v.size() / 3, nn = (int64_t)o->n.size() / 3;
+  for (size_t k = 0; k < o->vi.size(); k++)
+    if (o->vi[k] < 0 || o->vi[k] >= nv || o->ni[k] < 0 || o->ni[k] >= nn) {
+      delete o;
+      return fail("face index out of range");
+    }
+  *out = o;
+  return CRT_OK;
+}
+
+crt_status crt_obj_mesh(const crt_obj* o, crt_mesh_desc* mesh) {
+  if (!o || !mesh) return fail("null argument");
+  mesh->vertices = o->v.data();
+  mesh->num_vertices = (int32_t)(o->v.size() / 3);
+  mesh->normals = o->n.data();
+  mesh->num_normals = (int32_t)(o->n.size() / 3);
+  mesh->vertex_indices = o->vi.data();
+  mesh->normal_indices = o->ni.data();
+  mesh->num_triangles = (int32_t)o->mid.size();
+  mesh->materials = o->mats.data();
+  mesh->num_materials = (int32_t)o->mats.size();
+  mesh->material_ids = o->mid.data();
+  return CRT_OK;
+}
+
+crt_status crt_obj_free(crt_obj* o) {
+  delete o;
+  return CRT_OK;
+}
+
+crt_status crt_write_bmp(const char* path, int32_t width, int32_t height, const uint8_t* rgb8) {
+  if (!path || !rgb8 || width <= 0 || height <= 0) return fail("bad arguments");
+  const int row = width * 3, pad = (row % 4) ? 4 - row % 4 : 0;
+  const uint32_t image = (uint32_t)(row + pad) * (uint32_t)height;
+  uint8_t h[54];
+  std::memset(h, 0, sizeof(h));
+  auto u16 = [&](int at, uint32_t v) { h[at] = v & 0xff, h[at + 1] = (v >> 8) & 0xff; };
+  auto u32 = [&](int at, uint32_t v) {
+    for (int k = 0; k < 4; k++) h[at + k] = (v >> (8 * k)) & 0xff;
+  };
+  u16(0, 0x4d42);       // "BM"
+  u32(2, 54 + image);   // file size
+  u32(10, 54);          // pixel data offset
+  u32(14, 40);          // info header size
+  u32(18, (uint32_t)width);
+  u32(22, (uint32_t)height);
+  u16(26, 1);           // planes
+  u16(28, 24);          // bits per pixel
+  u32(38, (uint32_t)(100 / 2.54 * 72));  // pixels per metre, x and y
+  u32(42, (uint32_t)(100 / 2.54 * 72));
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(std::string("cannot write ") + path);
+  bool ok = std::fwrite(h, 1, sizeof(h), f) == sizeof(h);
+  std::vector<uint8_t> line(row + pad, 0);
+  for (int j = 0; j < height && ok; j++) {  // rows bottom-up, as the image buffer
+    const uint8_t* src = rgb8 + (size_t)j * row;
+    for (int i = 0; i < width; i++) {
+      line[3 * i] = src[3 * i + 2];
+      line[3 * i + 1] = src[3 * i + 1];
+      line[3 * i + 2] = src[3 * i];
+    }
+    ok = std::fwrite(line.data(), 1, line.size(), f) == line.size();
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? CRT_OK : fail(std::string("write failed: ") + path);
+}
+
+}  // extern "C"

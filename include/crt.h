@@ -259,6 +259,24 @@ crt_status crt_batch_export(crt_batch* batch, int32_t mesh, float* scene_box, in
 /* Synchronise `stream` and report device-side errors of the last run. */
 crt_status crt_batch_check(crt_batch* batch, void* stream);
 
+/* ---- scene input and image output of the drop-in CLI (host only).
+ * crt_obj_load reads a Wavefront OBJ and its MTL the way Scene_h::LoadObj
+ * does through tinyobjloader (src/scene.cpp:6-58): polygons
+ * fan-triangulated, per-face material ids (absent or unknown: material 0),
+ * Ka/Kd/Ks/Kt(Tf)/Ke/Ns with tinyobjloader's defaults.  Vertex and normal
+ * coordinates are rounded to FP32 (crt_mesh_desc's precision).  The MTL is
+ * looked up in mtl_dir (NULL: the OBJ's directory).  Every face corner must
+ * carry a normal index (the reference reads normals[-1] otherwise).
+ * crt_obj_mesh points a mesh description at the loaded arrays (valid until
+ * crt_obj_free). */
+typedef struct crt_obj crt_obj;
+crt_status crt_obj_load(const char* obj_path, const char* mtl_dir, crt_obj** out);
+crt_status crt_obj_mesh(const crt_obj* obj, crt_mesh_desc* mesh);
+crt_status crt_obj_free(crt_obj* obj);
+/* writeBMP (src/bitmap.cpp:99-154): 24-bit BMP of a host rgb8 image in
+ * crt_render_out's bottom-up order (rows padded to 4 bytes with zeros). */
+crt_status crt_write_bmp(const char* path, int32_t width, int32_t height, const uint8_t* rgb8);
+
 const char* crt_last_error_string(void);
 const char* crt_version(void);
 

@@ -552,10 +552,10 @@ int orc_render(void* h, const orc_camera* cam, const orc_light* light, int W, in
   const V3 eye = v3(cam->eye[0], cam->eye[1], cam->eye[2]);
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
-#pragma omp parallel for schedule(dynamic, 1) reduction(+ : overflow)
+#pragma omp parallel for collapse(2) schedule(dynamic, 64) reduction(+ : overflow)
 #endif
   for (int py = row0; py < row1; py++) {
-    for (int px = 0; px < W; px++) {
+    for (int px = 0; px < W; px++) {  // pixels are independent: all cores share any band of rows
       const int idx = (H - py - 1) * W + px;
       // getGlobalIdx_2D_2D (inc/indexing.h:4-9) for block (px/16, py/16),
       // thread (px%16, py%16); initPNRG seeds it with wangHash.

@@ -1,0 +1,95 @@
+"""The drop-in command-line renderer (crt_raytracer, the reference's cuda_bvh
+flags) end to end: OBJ/MTL in, BMP out, against the oracle's render of the
+same scene with the same camera and light (flag vectors parsed with float
+precision, as main.cpp's stof)."""
+import math
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import assert_equal
+from test_obj import read_bmp
+
+pytestmark = pytest.mark.gpu
+
+
+def write_scene(d, mesh):
+    with open(os.path.join(d, "soup.mtl"), "w") as f:
+        f.write("newmtl matte\nKd 0.8 0.7 0.6\nKs 0 0 0\n")
+    with open(os.path.join(d, "soup.obj"), "w") as f:
+        f.write("mtllib soup.mtl\n")
+        for v in mesh.verts:
+            f.write("v %.9g %.9g %.9g\n" % tuple(float(x) for x in v))
+        for n in mesh.normals:
+            f.write("vn %.9g %.9g %.9g\n" % tuple(float(x) for x in n))
+        f.write("usemtl matte\n")
+        for a, b in zip(mesh.vidx + 1, mesh.nidx + 1):
+            f.write("f %d//%d %d//%d %d//%d\n" % (a[0], b[0], a[1], b[1], a[2], b[2]))
+    return os.path.join(d, "soup.obj")
+
+
+def f32(*xs):
+    return tuple(float(np.float32(x)) for x in xs)
+
+
+@pytest.fixture(scope="module")
+def cli_scene(cuda, tmp_path_factory):
+    from crt import build, data
+    d = str(tmp_path_factory.mktemp("cli"))
+    mesh = data.soup(3000, seed=9, scale=0.9, cam_pos=(0.0, 0.0, -3.0))
+    obj = write_scene(d, mesh)
+    return build.build_cli(), d, obj, data.load_obj(obj)
+
+
+def run_cli(cli, args):
+    r = subprocess.run([cli] + args, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    return r
+
+
+def test_cli_pinhole_matches_oracle_bit_exact(cli_scene):
+    from crt import data
+    from oracle.oracle import OracleScene
+    cli, d, obj, mesh = cli_scene
+    bmp = os.path.join(d, "pinhole.bmp")
+    W, H, spp = 64, 48, 4
+    run_cli(cli, ["-i", obj, "-o", bmp, "-w", str(W), "-h", str(H), "-f", "inf", "-v", "45", "-P", "2",
+                  "-p", "2.3,1.7,-2.1", "-c", "1,0.9,0.8", "-a", "1,0,0.05", "-R", "0", "--spp", str(spp)])
+    got = read_bmp(bmp)
+    cam = data.Camera(fov=45.0, focal_point=2.0, fstop=math.inf)
+    light = data.Light(position=f32(2.3, 1.7, -2.1), color=f32(1, 0.9, 0.8), radius=0.0, constant_term=1.0,
+                       linear_term=0.0, quadratic_term=f32(0.05)[0])
+    ref = OracleScene(mesh).render(cam, light, W, H, spp=spp)["rgb"]
+    assert_equal(got, ref, "CLI image")
+    assert got.any()
+
+
+def test_cli_reference_defaults_thin_lens(cli_scene):
+    """The reference's defaults (fov 30, f-stop 8, focus 10, light at 1,1,1 with
+    falloff 0, 0.01, 0.001, 20 samples) with a point light (-R 0): thin-lens
+    rays use cos/sin, which may differ from the host's in the last bit, so
+    the image is held to 1/255 per channel."""
+    from crt import data
+    from oracle.oracle import OracleScene
+    cli, d, obj, mesh = cli_scene
+    bmp = os.path.join(d, "defaults.bmp")
+    run_cli(cli, ["--input=" + obj, "--output", bmp, "-w", "32", "-h", "32", "-R0"])
+    got = read_bmp(bmp)
+    cam = data.Camera(fov=30.0, focal_point=10.0, fstop=8.0)
+    light = data.Light(position=(1.0, 1.0, 1.0), color=(1.0, 1.0, 1.0), radius=0.0, constant_term=0.0,
+                       linear_term=0.01, quadratic_term=0.001)
+    ref = OracleScene(mesh).render(cam, light, 32, 32, spp=20)["rgb"]
+    diff = np.abs(got.astype(int) - ref.astype(int))
+    assert diff.max() <= 1 and (diff == 0).mean() > 0.99
+
+
+def test_cli_errors(cli_scene, tmp_path):
+    cli, d, obj, mesh = cli_scene
+    r = subprocess.run([cli, "-i", str(tmp_path / "absent.obj")], capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0 and "cannot open" in r.stderr
+    r = subprocess.run([cli, "-i", obj, "-w", "zero"], capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0 and "bad value" in r.stderr
+    r = subprocess.run([cli, "--bogus"], capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0

@@ -1,0 +1,105 @@
+"""Scene input and image output of the drop-in CLI, on the CPU: the library's
+OBJ/MTL reader (crt_obj_load) gives the same arrays as the reader the golden
+fixtures were made with (crt.data.load_obj), and crt_write_bmp writes the
+reference's 24-bit BMP layout (src/bitmap.cpp:99-154)."""
+import os
+import struct
+
+import numpy as np
+import pytest
+
+OBJ = """# a quad, a pentagon and loose triangles over two materials
+mtllib scene.mtl
+mtllib missing.mtl
+v 0 0 0
+v 1 0 0
+v 1 1 0
+v 0 1 0
+v 0.5 1.7 0.3
+v -0.25 0.125 2.0000001
+v 3.14159265358979 2.718281828 -1.41421356
+vn 0 0 1
+vn 0 1 0
+vn 0.577 0.577 0.577
+vt 0 0
+usemtl red
+f 1//1 2//1 3//1 4//1
+usemtl nosuchmaterial
+f 1/1/2 3/1/2 5/1/2
+usemtl glass
+f -1//-1 -2//-2 -3//-3 1//1 2//2
+f 6//3 7//3 5//3
+"""
+
+MTL = """newmtl red
+Ka 0.1 0.2 0.3
+Kd 0.8 0.1 0.1
+Ks 0.5 0.5 0.5
+Ns 32
+newmtl glass
+Kd 0.2 0.3 0.4
+Tf 0.9 0.9 0.9
+Ke 0.01 0.02 0.03
+"""
+
+
+@pytest.fixture()
+def scene_dir(tmp_path, built):
+    (tmp_path / "scene.obj").write_text(OBJ)
+    (tmp_path / "scene.mtl").write_text(MTL)
+    return tmp_path
+
+
+def test_native_reader_matches_python_reader(scene_dir):
+    import crt
+    from crt import data
+    a = crt.load_obj_native(str(scene_dir / "scene.obj"))
+    b = data.load_obj(str(scene_dir / "scene.obj"))
+    for k in ("verts", "vidx", "normals", "nidx", "matid", "materials"):
+        x, y = getattr(a, k), getattr(b, k)
+        assert x.dtype == y.dtype and x.shape == y.shape, k
+        assert np.array_equal(x, y), k
+    assert a.ntri == 2 + 1 + 3 + 1            # quad, triangle, pentagon (fan), triangle
+    assert list(a.matid) == [0, 0, 0, 1, 1, 1, 1]  # unknown material -> 0
+    assert a.materials[0, 15] == 32.0 and a.materials[1, 15] == 1.0  # tinyobjloader's default Ns
+    assert np.array_equal(a.materials[1, 9:12], [0.9, 0.9, 0.9])  # Tf is the transmittance
+
+
+def test_native_reader_rejects_faces_without_normals(tmp_path, built):
+    import crt
+    (tmp_path / "bad.obj").write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 3\n")
+    with pytest.raises(crt.CrtError, match="normal"):
+        crt.load_obj_native(str(tmp_path / "bad.obj"))
+    with pytest.raises(crt.CrtError, match="cannot open"):
+        crt.load_obj_native(str(tmp_path / "absent.obj"))
+    (tmp_path / "range.obj").write_text("v 0 0 0\nvn 0 0 1\nf 1//1 2//1 9//1\n")
+    with pytest.raises(crt.CrtError, match="out of range"):
+        crt.load_obj_native(str(tmp_path / "range.obj"))
+
+
+def test_default_material_without_mtl(tmp_path, built):
+    import crt
+    (tmp_path / "plain.obj").write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nvn 0 0 1\nf 1//1 2//1 3//1\n")
+    m = crt.load_obj_native(str(tmp_path / "plain.obj"))
+    assert m.materials.shape == (1, 16) and np.array_equal(m.materials[0, 3:6], [0.8, 0.8, 0.8])
+
+
+def read_bmp(path):
+    raw = open(path, "rb").read()
+    assert raw[:2] == b"BM"
+    size, off = struct.unpack_from("<I", raw, 2)[0], struct.unpack_from("<I", raw, 10)[0]
+    hsize, w, h, planes, bpp, comp = struct.unpack_from("<IiiHHI", raw, 14)
+    assert (size, off, hsize, planes, bpp, comp) == (len(raw), 54, 40, 1, 24, 0)
+    row = w * 3 + (-(w * 3) % 4)
+    px = np.frombuffer(raw[off:], np.uint8).reshape(h, row)[:, :w * 3].reshape(h, w, 3)
+    return px[..., ::-1].reshape(-1, 3)  # BGR -> RGB, rows in file order (bottom-up)
+
+
+@pytest.mark.parametrize("w,h", [(5, 3), (8, 2), (1, 1)])
+def test_bmp_layout(tmp_path, built, w, h):
+    import crt
+    rgb = np.random.default_rng(w * h).integers(0, 256, (w * h, 3), dtype=np.uint8)
+    path = str(tmp_path / "img.bmp")
+    crt.write_bmp(path, rgb, w, h)
+    assert os.path.getsize(path) == 54 + h * (w * 3 + (-(w * 3) % 4))
+    assert np.array_equal(read_bmp(path), rgb)
