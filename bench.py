@@ -211,6 +211,7 @@ def run_crt(args, dist, rank, ws):
 
     refit = run_refit_vs_rebuild() if (rank == 0 and not args.no_extras) else None
     batched = run_batched() if (rank == 0 and not args.no_extras) else None
+    adjoint = run_adjoint() if (rank == 0 and not args.no_extras) else None
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(sc, args.cpu_seconds)
@@ -242,6 +243,8 @@ def run_crt(args, dist, rank, ws):
         line["refit_vs_rebuild"] = refit
     if batched is not None:
         line["batched_vs_plain"] = batched
+    if adjoint is not None:
+        line["adjoint"] = adjoint
     if cpu is not None:
         line["cpu_baseline"] = cpu
     return line
@@ -353,6 +356,57 @@ def run_batched(count=256, reps=3):
             "plain_launches": 9 * count, "batched_launches": 12}
 
 
+def run_adjoint(reps=5):
+    """The differentiable workload: the 200,000-face icosphere with per-triangle
+    albedo, 512x512 at 4 spp, pinhole; L2 loss against the image of the
+    perturbed mesh.  Times one forward render (mean colour in double) and one
+    adjoint (d loss / d vertices, light, albedo) with CUDA events; the adjoint
+    re-traces every sample (nothing is stored between the two)."""
+    import torch
+
+    import crt
+    from crt import data
+    W = H = 512
+    spp = 4
+    sc = data.config4(width=W, height=H, spp=spp)
+    tgt = data.config4(width=W, height=H, spp=spp, perturbed=True)
+    stream = torch.cuda.current_stream()
+    g = crt.Scene(sc.mesh)
+    t_img = torch.empty((W * H, 3), dtype=torch.float64, device="cuda")
+    crt.Scene(tgt.mesh).render(tgt.camera, tgt.light, W, H, spp, out={"rgb_f64": t_img}, stream=stream)
+    img = torch.empty_like(t_img)
+    out = dict(vertices=torch.zeros((g.nv, 3), dtype=torch.float64, device="cuda"),
+               light=torch.zeros(3, dtype=torch.float64, device="cuda"),
+               kd=torch.zeros((g.nmat, 3), dtype=torch.float64, device="cuda"))
+
+    def fwd():
+        g.render(sc.camera, sc.light, W, H, spp, out={"rgb_f64": img}, stream=stream)
+
+    def bwd():
+        g.adjoint(sc.camera, sc.light, W, H, spp, 2.0 * (img - t_img), out=out, stream=stream)
+
+    fwd()
+    bwd()
+    torch.cuda.synchronize()
+    res = {}
+    for name, fn in (("forward", fwd), ("adjoint", bwd)):
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        res[name] = float(np.median(ts))
+    g.check()
+    rays = W * H * spp
+    return {"triangles": sc.mesh.ntri, "image": f"{W}x{H}x{spp}spp", "forward_ms": round(res["forward"], 3),
+            "adjoint_ms": round(res["adjoint"], 3), "forward_mrays_s": round(rays / res["forward"] / 1e3, 1),
+            "adjoint_mrays_s": round(rays / res["adjoint"] / 1e3, 1),
+            "loss": round(float(((img - t_img) ** 2).sum()), 6)}
+
+
 def _cpu_impl():
     from oracle import oracle as orc
     kind = "port"
@@ -429,7 +483,7 @@ def main():
     ap.add_argument("--impl", default="crt", choices=["crt", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-extras", action="store_true", help="skip the refit-vs-rebuild and batched-vs-plain figures")
+    ap.add_argument("--no-extras", action="store_true", help="skip the refit-vs-rebuild, batched-vs-plain and adjoint figures")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "crt" else args.warmup
     dist, rank, ws = dist_setup()
