@@ -11,6 +11,7 @@
 // taken by an *_exact routine.
 #pragma once
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 namespace crt {
@@ -354,31 +355,45 @@ struct TravStats {
 };
 // The traversal stack: entries live in local memory, or (SHORT > 0) the top
 // SHORT entries in a per-thread shared-memory ring (slot i of thread t at
-// ring[i * blockDim.x]) with older entries spilled to local memory.
-template <int SHORT>
+// ring[i * blockDim.x], int2 slots) with older entries spilled to local
+// memory.  E is int2 (node, pruning bound) for closest hits and int (node)
+// for any hits.
+__device__ __forceinline__ int2 to_slot(int2 e) { return e; }
+__device__ __forceinline__ int2 to_slot(int e) { return make_int2(e, 0); }
+__device__ __forceinline__ void from_slot(int2 s, int2& e) { e = s; }
+__device__ __forceinline__ void from_slot(int2 s, int& e) { e = s.x; }
+template <int SHORT, typename E>
 struct TravStack {
-  int2 local[kWideStack];
+  E local[kWideStack];
   int2* ring;
   int sp = 0;
-  __device__ __forceinline__ void push(int2 e) {
+  __device__ __forceinline__ void push(E e) {
     if (SHORT == 0) {
       local[sp++] = e;
       return;
     }
     const int slot = (sp & (SHORT - 1)) * (int)blockDim.x;
-    if (sp >= SHORT) local[sp - SHORT] = ring[slot];
-    ring[slot] = e;
+    if (sp >= SHORT) from_slot(ring[slot], local[sp - SHORT]);
+    ring[slot] = to_slot(e);
     sp++;
   }
-  __device__ __forceinline__ int2 pop() {
+  __device__ __forceinline__ E pop() {
     --sp;
     if (SHORT == 0) return local[sp];
     const int slot = (sp & (SHORT - 1)) * (int)blockDim.x;
-    const int2 e = ring[slot];
-    if (sp >= SHORT) ring[slot] = local[sp - SHORT];
+    E e;
+    from_slot(ring[slot], e);
+    if (sp >= SHORT) ring[slot] = to_slot(local[sp - SHORT]);
     return e;
   }
 };
+
+__device__ __forceinline__ int2 stack_entry(int node, float t, int2*) { return make_int2(node, __float_as_int(t)); }
+__device__ __forceinline__ int stack_entry(int node, float, int*) { return node; }
+__device__ __forceinline__ int entry_node(int2 e) { return e.x; }
+__device__ __forceinline__ int entry_node(int e) { return e; }
+__device__ __forceinline__ float entry_bound(int2 e) { return __int_as_float(e.y); }
+__device__ __forceinline__ float entry_bound(int) { return 0.f; }
 
 // Leaf codes carry a flag: bit 30 of ~code set = the leaf's box passed the
 // conservative filter but not the certain one, so its exact box test is
@@ -415,23 +430,24 @@ __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, const fl
   int node = S.root;
   if (node < 0 && !box_sure(r, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5])) node = ~kLeafBoxDue;
   float pb = __int_as_float(0x7f800000);  // prune bound; +inf until a hit
-  TravStack<SHORT> stk;
+  using E = typename std::conditional<ANY, int, int2>::type;
+  TravStack<SHORT, E> stk;
   stk.ring = ring;
   int cand = 0;  // the pending candidate's leaf code (with its box flag)
   bool pending = false;
   // a valid tree visits each node at most once per ray; the bound and the
   // index checks only guard against a corrupt tree
-  const int64_t max_steps = 2 * (int64_t)S.ntri + 64;
-  int64_t steps = 0;
+  const int max_steps = 2 * S.ntri + 64;  // < 2^31 below CRT_MAX_TRIANGLES
+  int steps = 0;
   while (true) {
     // FP32 phase: this lane's next candidate
     while (run && !pending) {
       if (node == kPop) {
         bool next = false;
         while (stk.sp > 0) {
-          const int2 e = stk.pop();
-          if (!ANY && __int_as_float(e.y) > pb) continue;
-          node = e.x;
+          const E e = stk.pop();
+          if (!ANY && entry_bound(e) > pb) continue;
+          node = entry_node(e);
           next = true;
           break;
         }
@@ -484,7 +500,7 @@ __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, const fl
 #pragma unroll
         for (int k = 3; k >= 0; k--) {
           if (c[k] != kNoChild) {
-            if (next != kPop) stk.push(make_int2(next, __float_as_int(tnext)));
+            if (next != kPop) stk.push(stack_entry(next, tnext, (E*)nullptr));
             next = c[k];
             tnext = t[k];
           }

@@ -139,7 +139,11 @@ __device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int 
           const double dofRadius = A.aperture * sqrt(rand_double(st)) / 2.0;
           org = d3(0.0, 0.0, 0.0);
           if (dofRadius != 0.0) {  // a zero radius gives +-0 components, which no later operation can tell apart
-            org = d3(dofRadius * cos(dofAngle), dofRadius * sin(dofAngle), 0.0);
+            // sincos gives sin and cos bit for bit (checked for every angle 2*pi*u
+            // the float-valued mrand draw u can take)
+            double sa, ca;
+            sincos(dofAngle, &sa, &ca);
+            org = d3(dofRadius * ca, dofRadius * sa, 0.0);
           }
           dir = normalize_exact(fdir - org);
           ray_setup(rc, org.x, org.y, org.z, dir.x, dir.y, dir.z, B, D);

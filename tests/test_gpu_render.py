@@ -119,3 +119,29 @@ def test_render_non_multiple_of_16(cuda):
     o = OracleScene(sc.mesh).render(sc.camera, sc.light, W, H, spp=3, aux=True)
     assert_equal(out["hit_id"], o["hit_id"], "hit id")
     assert_equal(out["rgb8"], o["rgb"], "rgb8")
+
+
+@pytest.mark.parametrize("spp", [2, 3, 5, 7, 33])
+def test_dof_sample_counts_with_partial_waves(cuda, spp):
+    """Sample counts that are not a multiple of the lanes a pixel takes (the
+    last wave is partial) and one above 32; thin lens on the silhouette of the
+    large mesh, where samples of one pixel mix hits and misses, so the guesses
+    of the stream offsets are wrong and re-traced.  Replayed rays give the
+    oracle's hits and image bit for bit."""
+    import crt
+    from crt import data
+    from oracle.oracle import OracleScene
+    sc = data.config1()
+    W, H = 48, 40
+    g = crt.Scene(sc.mesh)
+    out = g.render(sc.camera, sc.light, W, H, spp, aux=True, rays=True)
+    o = OracleScene(sc.mesh)
+    own = o.render(sc.camera, sc.light, W, H, spp=spp, rays_out=True)
+    assert np.allclose(out["rays"], own["rays"], rtol=2.0 ** -21, atol=1e-15)
+    rep = o.render(sc.camera, sc.light, W, H, spp=spp, rays_in=out["rays"], aux=True)
+    assert_equal(out["hit_id"], rep["hit_id"], "hit id")
+    assert_equal(out["shadow"], rep["shadow"], "shadow")
+    assert_equal(out["rgb8"], rep["rgb"], "rgb8")
+    hits = (out["hit_id"].reshape(W * H, spp) >= 0)
+    assert (hits.any(1) & ~hits.all(1)).any(), "no pixel mixes hits and misses"
+    g.check()
