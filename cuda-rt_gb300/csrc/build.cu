@@ -485,7 +485,8 @@ constexpr uint32_t kParentLeft = 1u << 31, kParentSpans = 1u << 30, kParentMask 
 // children's parent words and clears the node's refit flag (the child codes
 // reach the wide nodes through the refit, with the boxes).
 __global__ void __launch_bounds__(256) k_hierarchy(const uint32_t* __restrict__ codes, int n,
-                                                   uint32_t* __restrict__ parent, int* __restrict__ flags) {
+                                                   uint32_t* __restrict__ parent, int* __restrict__ flags,
+                                                   WNode* __restrict__ wnodes) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n - 1) return;
   const uint64_t ki = ((uint64_t)__ldg(codes + i) << 32) | (uint32_t)i;
@@ -519,6 +520,10 @@ __global__ void __launch_bounds__(256) k_hierarchy(const uint32_t* __restrict__ 
   parent[c1 < 0 ? (n - 1) + split : split] = (uint32_t)i | kParentLeft | spans;
   parent[c2 < 0 ? (n - 1) + split + 1 : split + 1] = (uint32_t)i | spans;
   flags[i] = 0;
+  // a leaf child takes one slot of this node's wide node: mark the other empty
+  const float4 empty = make_float4(0.f, 0.f, 0.f, __int_as_float(kNoChild));
+  if (c1 < 0) wnodes[i].s[1].lo_code = empty;
+  if (c2 < 0) wnodes[i].s[3].lo_code = empty;
 }
 
 // RefitBounds (kernels/bvh.cu:209-258): one climber per leaf; at each node the
@@ -527,8 +532,8 @@ __global__ void __launch_bounds__(256) k_hierarchy(const uint32_t* __restrict__ 
 // reference's boxes.  Every box goes to the wide nodes (WNode): child x (code
 // xc) of binary node p fills slot 2*side(p) + side(x) of the wide node of p's
 // parent gp (for the root, the virtual node past the last internal one), and
-// a leaf child also fills its own slot of p's wide node, with the odd slot
-// marked empty.  Codes are rewritten with the boxes, so a refit alone keeps
+// a leaf child also fills its own slot of p's wide node (the hierarchy marks
+// the odd slot empty).  Codes are rewritten with the boxes, so a refit alone keeps
 // the wide nodes complete, and the children of every node can be read back
 // from its parent's wide node (the export does).
 //
@@ -545,11 +550,10 @@ __device__ __forceinline__ void put_wide(WNode* W, int xc, bool x_left, int p, i
                                          const float lo[3], const float hi[3]) {
   const float4 a = make_float4(lo[0], lo[1], lo[2], __int_as_float(xc));
   const float4 b = make_float4(hi[0], hi[1], hi[2], 0.f);
-  if (xc < 0) {
+  if (xc < 0) {  // (the hierarchy marked the odd slot empty)
     WSlot* q = W[p].s + (x_left ? 0 : 2);
     __stcg(&q[0].lo_code, a);
     __stcg(&q[0].hi, b);
-    __stcg(&q[1].lo_code, make_float4(0.f, 0.f, 0.f, __int_as_float(kNoChild)));
   }
   WSlot* q = W[gp].s + (p_left ? 0 : 2) + (x_left ? 0 : 1);
   __stcg(&q->lo_code, a);
@@ -570,7 +574,7 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__
                                                        WNode* wnodes, LeafTri* __restrict__ leaves,
                                                        const uint32_t* __restrict__ parent, int* flags,
                                                        SceneGlobals* g) {
-  __shared__ float s_box[kRefitBlock][2][6];  // children's boxes at each block-local node
+  __shared__ float4 s_box[kRefitBlock][2][2];  // children's boxes at each block-local node (lo, hi)
   __shared__ int s_flag[kRefitBlock];
   s_flag[threadIdx.x] = 0;
   __syncthreads();
@@ -613,15 +617,16 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__
         put_wide(wnodes, xc, is_left, p, gp, p_left, lo, hi);
         if (!(w & kParentSpans)) {  // both arrivals are threads of this block
           const int sl = p - k0;
-          float* mine = s_box[sl][is_left ? 0 : 1];
-#pragma unroll
-          for (int q = 0; q < 3; q++) mine[q] = lo[q], mine[3 + q] = hi[q];
+          float4* mine = s_box[sl][is_left ? 0 : 1];
+          mine[0] = make_float4(lo[0], lo[1], lo[2], 0.f);
+          mine[1] = make_float4(hi[0], hi[1], hi[2], 0.f);
           __threadfence_block();
           if (atomicAdd(&s_flag[sl], 1) == 0) break;  // first arrival
           __threadfence_block();
-          const volatile float* o = s_box[sl][is_left ? 1 : 0];
-#pragma unroll
-          for (int q = 0; q < 3; q++) lo[q] = fminf(lo[q], o[q]), hi[q] = fmaxf(hi[q], o[3 + q]);
+          const float4* o = s_box[sl][is_left ? 1 : 0];
+          const float4 ol = o[0], oh = o[1];
+          lo[0] = fminf(lo[0], ol.x), lo[1] = fminf(lo[1], ol.y), lo[2] = fminf(lo[2], ol.z);
+          hi[0] = fmaxf(hi[0], oh.x), hi[1] = fmaxf(hi[1], oh.y), hi[2] = fmaxf(hi[2], oh.z);
         } else {
           // spanning node: release our slot, acquire the sibling's (gpu scope)
           if ((atomic_add_acq_rel(flags + p, 1) & 1) == 0) break;  // first arrival
@@ -770,7 +775,7 @@ __device__ __forceinline__ int mesh_of_internal(const int* __restrict__ tri_off,
 __global__ void __launch_bounds__(256) k_hierarchy_batch(const uint32_t* __restrict__ codes_all,
                                                          const int* __restrict__ tri_off, int M, int NI,
                                                          uint32_t* __restrict__ parent,
-                                                         int* __restrict__ flags) {
+                                                         int* __restrict__ flags, WNode* __restrict__ wnodes) {
   const int gi = blockIdx.x * blockDim.x + threadIdx.x;
   if (gi >= NI) return;
   int m = mesh_of_internal(tri_off, M, gi);
@@ -812,6 +817,9 @@ __global__ void __launch_bounds__(256) k_hierarchy_batch(const uint32_t* __restr
   parent[c1 < 0 ? NI + t0 + split : ib + split] = (uint32_t)gi | kParentLeft | spans;
   parent[c2 < 0 ? NI + t0 + split + 1 : ib + split + 1] = (uint32_t)gi | spans;
   flags[gi] = 0;
+  const float4 empty = make_float4(0.f, 0.f, 0.f, __int_as_float(kNoChild));
+  if (c1 < 0) wnodes[gi].s[1].lo_code = empty;
+  if (c2 < 0) wnodes[gi].s[3].lo_code = empty;
 }
 
 // RefitBounds per mesh; leaves at global sorted positions, the block-local /
@@ -824,7 +832,7 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit_batch(const float* __rest
                                                              WNode* wnodes, LeafTri* __restrict__ leaves,
                                                              const uint32_t* __restrict__ parent, int* flags,
                                                              SceneGlobals* g) {
-  __shared__ float s_box[kRefitBlock][2][6];
+  __shared__ float4 s_box[kRefitBlock][2][2];
   __shared__ int s_flag[kRefitBlock];
   s_flag[threadIdx.x] = 0;
   __syncthreads();
@@ -868,15 +876,16 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit_batch(const float* __rest
     put_wide(wnodes, xc, is_left, p, gp, p_left, lo, hi);
     if (!(w & kParentSpans)) {
       const int sl = p + m - k0;  // global leaf position of the node's index, within this block
-      float* mine = s_box[sl][is_left ? 0 : 1];
-#pragma unroll
-      for (int q = 0; q < 3; q++) mine[q] = lo[q], mine[3 + q] = hi[q];
+      float4* mine = s_box[sl][is_left ? 0 : 1];
+      mine[0] = make_float4(lo[0], lo[1], lo[2], 0.f);
+      mine[1] = make_float4(hi[0], hi[1], hi[2], 0.f);
       __threadfence_block();
       if (atomicAdd(&s_flag[sl], 1) == 0) return;
       __threadfence_block();
-      const volatile float* o = s_box[sl][is_left ? 1 : 0];
-#pragma unroll
-      for (int q = 0; q < 3; q++) lo[q] = fminf(lo[q], o[q]), hi[q] = fmaxf(hi[q], o[3 + q]);
+      const float4* o = s_box[sl][is_left ? 1 : 0];
+      const float4 ol = o[0], oh = o[1];
+      lo[0] = fminf(lo[0], ol.x), lo[1] = fminf(lo[1], ol.y), lo[2] = fminf(lo[2], ol.z);
+      hi[0] = fmaxf(hi[0], oh.x), hi[1] = fmaxf(hi[1], oh.y), hi[2] = fmaxf(hi[2], oh.z);
     } else {
       if ((atomic_add_acq_rel(flags + p, 1) & 1) == 0) return;
       sibling_box(wnodes, gp, p_left, is_left, lo, hi);
@@ -939,7 +948,7 @@ cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st)
     kin = ko;
     vin = vo;
   }
-  if (n >= 2) k_hierarchy<<<(n - 1 + 255) / 256, 256, 0, st>>>(b.keys_b, n, b.parent, b.flags);
+  if (n >= 2) k_hierarchy<<<(n - 1 + 255) / 256, 256, 0, st>>>(b.keys_b, n, b.parent, b.flags, b.wnodes);
   refit(m, b, st);
   return cudaGetLastError();
 }
@@ -973,7 +982,8 @@ cudaError_t launch_build_batch(const BatchBufs& b, cudaStream_t st) {
                                               b.status + (size_t)3 * tiles * kRadix, b.counters + 3, b.err);
   k_gather_codes<<<ge, 256, 0, st>>>(b.vals_a, b.codes0, N, b.keys_b);
   if (b.NI > 0)
-    k_hierarchy_batch<<<(b.NI + 255) / 256, 256, 0, st>>>(b.keys_b, b.tri_off, M, b.NI, b.parent, b.flags);
+    k_hierarchy_batch<<<(b.NI + 255) / 256, 256, 0, st>>>(b.keys_b, b.tri_off, M, b.NI, b.parent, b.flags,
+                                                          b.wnodes);
   k_refit_batch<<<(N + kRefitBlock - 1) / kRefitBlock, kRefitBlock, 0, st>>>(
       b.verts, b.vidx, b.vals_a, b.mesh_of, b.tri_off, N, b.NI, b.wnodes, b.leaves, b.parent, b.flags, b.g);
   return cudaGetLastError();
