@@ -201,7 +201,7 @@ __device__ __forceinline__ void load_scene_box(const SceneGlobals* g, float mn[3
 }
 
 // Morton codes + per-pass digit histograms; also clears the look-back status.
-__global__ void __launch_bounds__(512) k_morton(const float* __restrict__ V, const int* __restrict__ vidx, int n,
+__global__ void __launch_bounds__(512, 2) k_morton(const float* __restrict__ V, const int* __restrict__ vidx, int n,
                                                 const SceneGlobals* g, uint32_t* __restrict__ keys,
                                                 uint32_t* __restrict__ hist, int passes,
                                                 uint32_t* __restrict__ status, int status_words) {
@@ -722,7 +722,7 @@ __global__ void __launch_bounds__(256) k_bounds_batch(const float* __restrict__ 
 
 // Morton codes against each triangle's own mesh box, a copy of the codes,
 // the digit histograms of the three code passes; clears the look-back status.
-__global__ void __launch_bounds__(512) k_morton_batch(const float* __restrict__ V, const int* __restrict__ vidx,
+__global__ void __launch_bounds__(512, 2) k_morton_batch(const float* __restrict__ V, const int* __restrict__ vidx,
                                                       const int* __restrict__ mesh_of, int N,
                                                       const SceneGlobals* __restrict__ g, uint32_t* __restrict__ keys,
                                                       uint32_t* __restrict__ codes0, uint32_t* __restrict__ hist,
