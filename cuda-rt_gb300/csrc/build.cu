@@ -582,8 +582,10 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__
   const int k = k0 + threadIdx.x;
   float e = 0.f;
   bool ok = true;
-  if (k < n) {
-    const int tri = (int)__ldg(ids + k);
+  const int tri = k < n ? (int)__ldg(ids + k) : 0;
+  if (k < n && (unsigned)tri >= (unsigned)n) {  // only a corrupt sort gets here
+    atomicOr(&g->err, kErrStack);
+  } else if (k < n) {
     float3 a, b, c;
     float lo[3], hi[3];
     tri_box(V, vidx, tri, a, b, c, lo, hi);
@@ -840,6 +842,10 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit_batch(const float* __rest
   const int k = k0 + threadIdx.x;
   if (k >= N) return;
   const int tri = (int)__ldg(ids + k);
+  if ((unsigned)tri >= (unsigned)N) {  // only a corrupt sort gets here
+    atomicOr(&g[0].err, kErrStack);
+    return;
+  }
   const int m = __ldg(mesh_of + tri);
   const int t0 = __ldg(tri_off + m);
   const int n = __ldg(tri_off + m + 1) - t0;
