@@ -53,6 +53,7 @@ __global__ void k_build_init(SceneGlobals* g, uint32_t* hist, int nhist) {
   if (t == 0) {
     g->emax = f2ord(0.f);
     g->err = 0;
+    g->narr = 0u;
   }
   if (t < 4) g->tile_counter[t] = 0;
   for (int i = t; i < nhist; i += blockDim.x) hist[i] = 0;
@@ -569,11 +570,73 @@ __device__ __forceinline__ void sibling_box(const WNode* W, int gp, bool p_left,
   hi[0] = fmaxf(hi[0], b.x), hi[1] = fmaxf(hi[1], b.y), hi[2] = fmaxf(hi[2], b.z);
 }
 
+// The climb through the spanning nodes (leaf ranges over several blocks),
+// after k_refit stopped every climber at its first spanning parent and
+// recorded the arrival (its parent word; its box is in the wide node).  Each
+// arrival meets its sibling at gpu scope: a release/acquire add on the
+// parent's flag, whose parity tells the second arrival, which takes the union
+// and climbs on.  Spanning nodes have spanning parents, so every further
+// step meets the same way.  A separate launch keeps k_refit's blocks from
+// being held by a few long climbs.
+__global__ void __launch_bounds__(256) k_refit_top(WNode* wnodes, const uint32_t* __restrict__ parent,
+                                                   const uint32_t* __restrict__ arrivals, int n, int* flags,
+                                                   SceneGlobals* g) {
+  const unsigned count = *(volatile unsigned*)&g->narr;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    uint32_t w = __ldg(arrivals + i);
+    int p = (int)(w & kParentMask);
+    if (p >= n - 1) {  // only a corrupt tree gets here
+      atomicOr(&g->err, kErrStack);
+      continue;
+    }
+    uint32_t wn = (p == 0) ? 0u : __ldg(parent + p);
+    bool is_left = (w & kParentLeft) != 0;
+    int gp = (p == 0) ? n - 1 : (int)(wn & kParentMask);
+    bool p_left = (p == 0) || (wn & kParentLeft) != 0;
+    if (p != 0 && gp >= n - 1) {
+      atomicOr(&g->err, kErrStack);
+      continue;
+    }
+    float lo[3], hi[3];
+    {
+      const WSlot* q = wnodes[gp].s + (p_left ? 0 : 2) + (is_left ? 0 : 1);
+      const float4 a = __ldcg(&q->lo_code), b = __ldcg(&q->hi);
+      lo[0] = a.x, lo[1] = a.y, lo[2] = a.z, hi[0] = b.x, hi[1] = b.y, hi[2] = b.z;
+    }
+    for (int level = 0;; level++) {
+      if ((atomic_add_acq_rel(flags + p, 1) & 1) == 0) break;  // first arrival
+      sibling_box(wnodes, gp, p_left, is_left, lo, hi);
+      if (p == 0) {
+#pragma unroll
+        for (int q = 0; q < 3; q++) g->root_box[q] = lo[q], g->root_box[3 + q] = hi[q];
+        break;
+      }
+      // climb: p's box becomes a child slot one level up
+      const int xc = p;
+      w = wn;
+      p = (int)(w & kParentMask);
+      if (level >= kStackSize || p >= n - 1) {  // only a corrupt tree gets here
+        atomicOr(&g->err, kErrStack);
+        break;
+      }
+      wn = (p == 0) ? 0u : __ldg(parent + p);
+      is_left = (w & kParentLeft) != 0;
+      gp = (p == 0) ? n - 1 : (int)(wn & kParentMask);
+      p_left = (p == 0) || (wn & kParentLeft) != 0;
+      if (gp >= n - 1 && p != 0) {
+        atomicOr(&g->err, kErrStack);
+        break;
+      }
+      put_wide(wnodes, xc, is_left, p, gp, p_left, lo, hi);
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__ V, const int* __restrict__ vidx,
                                                        const uint32_t* __restrict__ ids, int n,
                                                        WNode* wnodes, LeafTri* __restrict__ leaves,
-                                                       const uint32_t* __restrict__ parent, int* flags,
-                                                       SceneGlobals* g) {
+                                                       const uint32_t* __restrict__ parent,
+                                                       uint32_t* __restrict__ arrivals, SceneGlobals* g) {
   __shared__ float4 s_box[kRefitBlock][2][2];  // children's boxes at each block-local node (lo, hi)
   __shared__ int s_flag[kRefitBlock];
   s_flag[threadIdx.x] = 0;
@@ -630,9 +693,9 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__
           lo[0] = fminf(lo[0], ol.x), lo[1] = fminf(lo[1], ol.y), lo[2] = fminf(lo[2], ol.z);
           hi[0] = fmaxf(hi[0], oh.x), hi[1] = fmaxf(hi[1], oh.y), hi[2] = fmaxf(hi[2], oh.z);
         } else {
-          // spanning node: release our slot, acquire the sibling's (gpu scope)
-          if ((atomic_add_acq_rel(flags + p, 1) & 1) == 0) break;  // first arrival
-          sibling_box(wnodes, gp, p_left, is_left, lo, hi);
+          // spanning node: its climb continues in k_refit_top (its box is in the wide node)
+          arrivals[atomicAdd(&g->narr, 1u)] = w;
+          break;
         }
         if (p == 0) {
 #pragma unroll
@@ -910,13 +973,14 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit_batch(const float* __rest
 
 namespace {
 __global__ void k_refit_init(SceneGlobals* g) {
-  if (threadIdx.x == 0) g->emax = f2ord(0.f);
+  if (threadIdx.x == 0) g->emax = f2ord(0.f), g->narr = 0u;
 }
 
 void refit(const MeshBufs& m, const BuildBufs& b, cudaStream_t st) {
   const int n = m.ntri;
   k_refit<<<(n + kRefitBlock - 1) / kRefitBlock, kRefitBlock, 0, st>>>(m.verts, m.vidx, b.vals_b, n, b.wnodes,
-                                                                        b.leaves, b.parent, b.flags, b.g);
+                                                                        b.leaves, b.parent, b.arrivals, b.g);
+  if (n > kRefitBlock) k_refit_top<<<num_sms() * 2, 256, 0, st>>>(b.wnodes, b.parent, b.arrivals, n, b.flags, b.g);
 }
 }  // namespace
 

@@ -195,7 +195,8 @@ crt_status crt_scene_create(const crt_mesh_desc* d, void* stream, crt_scene** ou
   size_t off[11], total = 0;
   const size_t sizes[11] = {4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n, 4 * 3 * (size_t)kRadix,
                             4 * 3 * (size_t)tiles * kRadix, 4 * nn, 4 * (size_t)(n > 1 ? n - 1 : 1),
-                            0, sizeof(LeafTri) * (size_t)(n > 0 ? n : 1), sizeof(WNode) * (size_t)(n > 0 ? n : 1)};
+                            4 * (size_t)(n > 0 ? n : 1), sizeof(LeafTri) * (size_t)(n > 0 ? n : 1),
+                            sizeof(WNode) * (size_t)(n > 0 ? n : 1)};
   for (int i = 0; i < 11; i++) off[i] = total, total += align256(sizes[i]);
   const size_t goff = total;
   total += align256(sizeof(SceneGlobals));
@@ -211,6 +212,7 @@ crt_status crt_scene_create(const crt_mesh_desc* d, void* stream, crt_scene** ou
   b.status = reinterpret_cast<uint32_t*>(base + off[5]);
   b.parent = reinterpret_cast<uint32_t*>(base + off[6]);
   b.flags = reinterpret_cast<int*>(base + off[7]);
+  b.arrivals = reinterpret_cast<uint32_t*>(base + off[8]);
   b.leaves = reinterpret_cast<LeafTri*>(base + off[9]);
   b.wnodes = reinterpret_cast<WNode*>(base + off[10]);
   b.g = reinterpret_cast<SceneGlobals*>(base + goff);

@@ -26,6 +26,7 @@ struct BuildBufs {
   uint32_t* status = nullptr;  // 3 * tiles * kRadix
   uint32_t* parent = nullptr;  // 2n - 1: parent index (reference numbering) | left-child and spanning bits
   int* flags = nullptr;        // n - 1
+  uint32_t* arrivals = nullptr;  // n: climbs handed from the refit to its spanning-node pass
   WNode* wnodes = nullptr;     // n (the last one virtual: the root's children)
   LeafTri* leaves = nullptr;   // n
   SceneGlobals* g = nullptr;
