@@ -604,6 +604,8 @@ __global__ void __launch_bounds__(256) k_refit_top(WNode* wnodes, const uint32_t
       lo[0] = a.x, lo[1] = a.y, lo[2] = a.z, hi[0] = b.x, hi[1] = b.y, hi[2] = b.z;
     }
     for (int level = 0;; level++) {
+      // the next level's parent word, fetched while this level meets
+      const uint32_t wn_next = (p == 0) ? 0u : __ldg(parent + gp);
       if ((atomic_add_acq_rel(flags + p, 1) & 1) == 0) break;  // first arrival
       sibling_box(wnodes, gp, p_left, is_left, lo, hi);
       if (p == 0) {
@@ -619,7 +621,7 @@ __global__ void __launch_bounds__(256) k_refit_top(WNode* wnodes, const uint32_t
         atomicOr(&g->err, kErrStack);
         break;
       }
-      wn = (p == 0) ? 0u : __ldg(parent + p);
+      wn = wn_next;
       is_left = (w & kParentLeft) != 0;
       gp = (p == 0) ? n - 1 : (int)(wn & kParentMask);
       p_left = (p == 0) || (wn & kParentLeft) != 0;
