@@ -184,7 +184,7 @@ crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* v
                        5 * 4 * (size_t)N, 4 * 4 * (size_t)kRadix, 4 * 4 * (size_t)tiles * kRadix,
                        4 * (size_t)(NI + N), 4 * (size_t)(NI > 0 ? NI : 1), 0,
                        sizeof(LeafTri) * (size_t)N, sizeof(SceneGlobals) * (size_t)M, 64, b->image_bytes,
-                       sizeof(RenderArgs) * (size_t)M, sizeof(WNode) * (size_t)(NI + M)};
+                       sizeof(RenderArgs) * (size_t)M, sizeof(WNode) * (size_t)(NI + M), sizeof(uint2) * (size_t)N};
   const int K = sizeof(sz) / sizeof(sz[0]);
   std::vector<size_t> off(K);
   size_t total = 0;
@@ -222,6 +222,7 @@ crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* v
   b->image = (uint8_t*)at(18);
   b->args = (RenderArgs*)at(19);
   bb.wnodes = (WNode*)at(20);
+  bb.arrivals = (uint2*)at(21);
   BatchView& v = b->v;
   b->d_item_off = d_ioff;
   v.M = M, v.tri_off = d_toff;

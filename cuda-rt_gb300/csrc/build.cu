@@ -741,6 +741,7 @@ __global__ void k_batch_init(SceneGlobals* g, int M, uint32_t* hist, const int* 
     hist[i] = (p == 3 && d < M) ? (uint32_t)(tri_off[d + 1] - tri_off[d]) : 0u;
   }
   if (blockIdx.x == 0 && threadIdx.x < 4) counters[threadIdx.x] = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) counters[6] = 0;  // refit hand-offs
   if (blockIdx.x == 0 && threadIdx.x == 0) *err = 0;
 }
 
@@ -897,7 +898,8 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit_batch(const float* __rest
                                                              const int* __restrict__ mesh_of,
                                                              const int* __restrict__ tri_off, int N, int NI,
                                                              WNode* wnodes, LeafTri* __restrict__ leaves,
-                                                             const uint32_t* __restrict__ parent, int* flags,
+                                                             const uint32_t* __restrict__ parent,
+                                                             uint2* __restrict__ arrivals, unsigned* narr,
                                                              SceneGlobals* g) {
   __shared__ float4 s_box[kRefitBlock][2][2];
   __shared__ int s_flag[kRefitBlock];
@@ -957,9 +959,9 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit_batch(const float* __rest
       const float4 ol = o[0], oh = o[1];
       lo[0] = fminf(lo[0], ol.x), lo[1] = fminf(lo[1], ol.y), lo[2] = fminf(lo[2], ol.z);
       hi[0] = fmaxf(hi[0], oh.x), hi[1] = fmaxf(hi[1], oh.y), hi[2] = fmaxf(hi[2], oh.z);
-    } else {
-      if ((atomic_add_acq_rel(flags + p, 1) & 1) == 0) return;
-      sibling_box(wnodes, gp, p_left, is_left, lo, hi);
+    } else {  // spanning node: the climb continues in k_refit_top_batch
+      arrivals[atomicAdd(narr, 1u)] = make_uint2(w, (uint32_t)m);
+      return;
     }
     if (p == root) {
 #pragma unroll
@@ -968,6 +970,66 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit_batch(const float* __rest
     }
     xc = p - root;
     w = wn;
+  }
+}
+
+// k_refit_top per mesh (the arrival carries its mesh; codes are mesh-local).
+__global__ void __launch_bounds__(256) k_refit_top_batch(WNode* wnodes, const uint32_t* __restrict__ parent,
+                                                         const uint2* __restrict__ arrivals, const unsigned* narr,
+                                                         const int* __restrict__ tri_off, int M, int NI, int* flags,
+                                                         SceneGlobals* g) {
+  const unsigned count = *(const volatile unsigned*)narr;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+    const uint2 arr = __ldg(arrivals + i);
+    const int m = (int)arr.y;
+    if (m < 0 || m >= M) continue;  // only a corrupt arrival gets here
+    const int t0 = __ldg(tri_off + m), n = __ldg(tri_off + m + 1) - t0, root = t0 - m;
+    uint32_t w = arr.x;
+    int p = (int)(w & kParentMask);
+    if (p < root || p >= root + n - 1) {
+      atomicOr(&g[m].err, kErrStack);
+      continue;
+    }
+    uint32_t wn = (p == root) ? 0u : __ldg(parent + p);
+    bool is_left = (w & kParentLeft) != 0;
+    int gp = (p == root) ? NI + m : (int)(wn & kParentMask);
+    bool p_left = (p == root) || (wn & kParentLeft) != 0;
+    if (p != root && (gp < root || gp >= root + n - 1)) {
+      atomicOr(&g[m].err, kErrStack);
+      continue;
+    }
+    float lo[3], hi[3];
+    {
+      const WSlot* q = wnodes[gp].s + (p_left ? 0 : 2) + (is_left ? 0 : 1);
+      const float4 a = __ldcg(&q->lo_code), b = __ldcg(&q->hi);
+      lo[0] = a.x, lo[1] = a.y, lo[2] = a.z, hi[0] = b.x, hi[1] = b.y, hi[2] = b.z;
+    }
+    for (int level = 0;; level++) {
+      const uint32_t wn_next = (p == root) ? 0u : __ldg(parent + gp);
+      if ((atomic_add_acq_rel(flags + p, 1) & 1) == 0) break;  // first arrival
+      sibling_box(wnodes, gp, p_left, is_left, lo, hi);
+      if (p == root) {
+#pragma unroll
+        for (int q = 0; q < 3; q++) g[m].root_box[q] = lo[q], g[m].root_box[3 + q] = hi[q];
+        break;
+      }
+      const int xc = p - root;
+      w = wn;
+      p = (int)(w & kParentMask);
+      if (level >= kStackSize || p < root || p >= root + n - 1) {
+        atomicOr(&g[m].err, kErrStack);
+        break;
+      }
+      wn = wn_next;
+      is_left = (w & kParentLeft) != 0;
+      gp = (p == root) ? NI + m : (int)(wn & kParentMask);
+      p_left = (p == root) || (wn & kParentLeft) != 0;
+      if (p != root && (gp < root || gp >= root + n - 1)) {
+        atomicOr(&g[m].err, kErrStack);
+        break;
+      }
+      put_wide(wnodes, xc, is_left, p, gp, p_left, lo, hi);
+    }
   }
 }
 
@@ -1057,7 +1119,11 @@ cudaError_t launch_build_batch(const BatchBufs& b, cudaStream_t st) {
     k_hierarchy_batch<<<(b.NI + 255) / 256, 256, 0, st>>>(b.keys_b, b.tri_off, M, b.NI, b.parent, b.flags,
                                                           b.wnodes);
   k_refit_batch<<<(N + kRefitBlock - 1) / kRefitBlock, kRefitBlock, 0, st>>>(
-      b.verts, b.vidx, b.vals_a, b.mesh_of, b.tri_off, N, b.NI, b.wnodes, b.leaves, b.parent, b.flags, b.g);
+      b.verts, b.vidx, b.vals_a, b.mesh_of, b.tri_off, N, b.NI, b.wnodes, b.leaves, b.parent, b.arrivals,
+      b.counters + 6, b.g);
+  if (N > kRefitBlock)
+    k_refit_top_batch<<<num_sms() * 2, 256, 0, st>>>(b.wnodes, b.parent, b.arrivals, b.counters + 6, b.tri_off, M,
+                                                      b.NI, b.flags, b.g);
   return cudaGetLastError();
 }
 

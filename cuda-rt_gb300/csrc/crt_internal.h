@@ -58,7 +58,8 @@ struct BatchBufs {
   WNode* wnodes = nullptr;     // NI + M (codes local to each mesh; NI + m: mesh m's virtual node)
   LeafTri* leaves = nullptr;   // N
   SceneGlobals* g = nullptr;   // M
-  unsigned* counters = nullptr;  // 4
+  unsigned* counters = nullptr;  // [0..3] sort tiles, [4] render items, [6] refit hand-offs
+  uint2* arrivals = nullptr;     // N: climbs handed from the refit to its spanning-node pass
   int* err = nullptr;
 };
 
