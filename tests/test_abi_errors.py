@@ -1,0 +1,83 @@
+"""Argument checking of the C ABI, on the CPU: every call below is refused
+before the library touches the GPU, with CRT_INVALID_ARG and a message in
+crt_last_error_string(), and nothing exits the process (the reference calls
+exit(1) on errors, src/scene.cpp:71-81)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+INVALID = 1
+
+
+@pytest.fixture()
+def lib(built):
+    import crt
+    return crt.lib()
+
+
+def desc(n, nv=3, nn=1, nmat=1, verts=True, mats=True):
+    import crt
+    keep = [np.zeros(3 * max(nv, 1), np.float32), np.zeros(3 * max(nn, 1), np.float32),
+            np.zeros(3 * max(min(n, 4), 1), np.int32), crt._Material()]
+    d = crt._MeshDesc(keep[0].ctypes.data if verts else None, nv, keep[1].ctypes.data, nn,
+                      keep[2].ctypes.data if verts else None, None, n,
+                      C.addressof(keep[3]) if mats else None, nmat, None)
+    return d, keep
+
+
+def error(lib):
+    return lib.crt_last_error_string().decode()
+
+
+def test_scene_create_refuses_bad_descriptions(lib):
+    out = C.c_void_p()
+    assert lib.crt_scene_create(None, None, C.byref(out)) == INVALID
+    d, keep = desc(n=(1 << 28) + 1)  # above CRT_MAX_TRIANGLES: refused before any index is read
+    assert lib.crt_scene_create(C.byref(d), None, C.byref(out)) == INVALID
+    assert "num_triangles" in error(lib)
+    d, keep = desc(n=-1)
+    assert lib.crt_scene_create(C.byref(d), None, C.byref(out)) == INVALID
+    d, keep = desc(n=1, nv=-3)
+    assert lib.crt_scene_create(C.byref(d), None, C.byref(out)) == INVALID and "negative" in error(lib)
+    d, keep = desc(n=1, verts=False)
+    assert lib.crt_scene_create(C.byref(d), None, C.byref(out)) == INVALID and "vertices" in error(lib)
+    d, keep = desc(n=1, mats=False)
+    assert lib.crt_scene_create(C.byref(d), None, C.byref(out)) == INVALID and "material" in error(lib)
+    assert not out.value
+
+
+def test_null_handles_are_refused(lib):
+    assert lib.crt_bvh_build(None, None) == INVALID
+    assert lib.crt_bvh_refit(None, None) == INVALID
+    assert lib.crt_scene_check(None, None) == INVALID
+    assert lib.crt_batch_check(None, None) == INVALID
+    assert lib.crt_batch_run(None, 1, None, None) == INVALID
+    assert lib.crt_scene_destroy(None) == 0 and lib.crt_batch_destroy(None) == 0
+
+
+def test_sort_refuses_bad_sizes(lib):
+    assert lib.crt_sort_pairs(None, None, None, None, 16, 0, None) == INVALID
+    assert lib.crt_sort_pairs(None, None, None, None, 16, 33, None) == INVALID
+    assert lib.crt_sort_pairs(None, None, None, None, -1, 30, None) == INVALID
+    assert lib.crt_sort_pairs(None, None, None, None, 0, 30, None) == 0  # nothing to sort
+    assert lib.crt_sort_pairs_noalloc(None, None, None, None, (1 << 20) + 1, 30, None) == INVALID
+
+
+def test_batch_create_refuses_bad_counts(lib):
+    import crt
+    out = C.c_void_p()
+    assert lib.crt_batch_create(None, None, 4, None, C.byref(out)) == INVALID
+    d, keep = desc(n=1)
+    descs = (crt._MeshDesc * 1025)(*([d] * 1025))
+    views = (crt._BatchView * 1025)()
+    assert lib.crt_batch_create(descs, views, 1025, None, C.byref(out)) == INVALID
+    assert "1024" in error(lib)
+    assert lib.crt_batch_create(descs, views, 0, None, C.byref(out)) == INVALID
+
+
+def test_loader_and_writer_refuse_bad_arguments(lib, tmp_path):
+    h = C.c_void_p()
+    assert lib.crt_obj_load(None, None, C.byref(h)) == INVALID
+    assert lib.crt_write_bmp(str(tmp_path / "x.bmp").encode(), 0, 4, None) == INVALID
+    assert lib.crt_obj_free(None) == 0
