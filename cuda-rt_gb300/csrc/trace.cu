@@ -383,7 +383,7 @@ __device__ __forceinline__ void flush_stats(const RenderArgs& A, const TravStats
 // SHORT: traversal-stack entries kept in shared memory per thread.
 constexpr int kPixelsShort = 0;
 template <int MODE>
-__global__ void __launch_bounds__(128, 4) k_pixels(DScene S, RenderArgs A) {
+__global__ void __launch_bounds__(128, 8) k_pixels(DScene S, RenderArgs A) {
   extern __shared__ int2 s_ring[];
   int2* ring = kPixelsShort > 0 ? s_ring + threadIdx.x : nullptr;
   TravStats ts;
@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(128, 4) k_pixels(DScene S, RenderArgs A) {
 // gmax) lanes each; SHORT is the shared-memory part of the traversal stack
 // (0: all local).
 template <int SHORT>
-__global__ void __launch_bounds__(256, 2) k_pixels_batch(BatchView V, int gmax) {
+__global__ void __launch_bounds__(256, 4) k_pixels_batch(BatchView V, int gmax) {
   extern __shared__ int2 s_ring[];
   int2* ring = SHORT > 0 ? s_ring + threadIdx.x : nullptr;
   TravStats ts;
