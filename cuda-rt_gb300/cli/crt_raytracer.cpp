@@ -1,7 +1,7 @@
 // crt_raytracer -- drop-in for the reference's cuda_bvh executable
 // (src/main.cpp:91-332): the same flags and defaults, an OBJ/MTL scene in, a
 // 24-bit BMP out, rendered by libcrt (crt_obj_load -> crt_scene_create ->
-// crt_render -> crt_write_bmp).
+// crt_render, or crt_render_recursive with --depth, -> crt_write_bmp).
 //
 //   -i, --input <file.obj>         scene (required); its MTL is read from the
 //                                  OBJ's directory, as main.cpp passes it
@@ -17,6 +17,10 @@
 //   -d, --orientation x,y,z        accepted; a positional light ignores it
 //   -n, --numeric, -1, --nonempty  accepted and ignored, as in main.cpp
 //       --spp <int>                samples per pixel (default 20, the reference's N)
+//       --depth <int>              levels of reflected and refracted rays (default 0:
+//                                  the reference's image, whose traceRay block for
+//                                  them is commented out; at most CRT_MAX_DEPTH),
+//                                  with kr = Ks and ior = Ni from the MTL
 //
 // Vectors are parsed per component with float precision and widened to
 // double, scalars with double precision, as main.cpp does (stof / stod).
@@ -44,12 +48,13 @@ const Opt kOpts[] = {{'i', "input", true},       {'o', "output", true},      {'w
                      {'P', "focalpoint", true},  {'p', "position", true},    {'c', "color", true},
                      {'a', "attenuation", true}, {'R', "radius", true},      {'d', "orientation", true},
                      {'n', "numeric", true},     {'1', "nonempty", true},    {0, "spp", true},
-                     {0, "help", false}};
+                     {0, "depth", true},         {0, "help", false}};
 
 void usage() {
   std::printf(
       "USAGE: crt_raytracer -i scene.obj -o image.bmp [-w W] [-h H] [-f fstop] [-v fov] [-P focal]\n"
-      "                     [-p x,y,z] [-c r,g,b] [-a a,b,c] [-R radius] [-d x,y,z] [--spp N]\n");
+      "                     [-p x,y,z] [-c r,g,b] [-a a,b,c] [-R radius] [-d x,y,z] [--spp N]\n"
+      "                     [--depth N]\n");
 }
 
 bool vec3(const std::string& s, double out[3]) {
@@ -83,7 +88,7 @@ int die(const char* what) {
 
 int main(int argc, char** argv) {
   std::string input, output;
-  int width = 512, height = 512, spp = 20;
+  int width = 512, height = 512, spp = 20, depth = 0;
   crt_camera cam{};
   cam.fov = 30.0, cam.fstop = 8.0, cam.focal_point = 10.0;  // Camera::Camera (kernels/camera.cu:10-22)
   crt_light light{};
@@ -135,6 +140,11 @@ int main(int argc, char** argv) {
       const long x = std::strtol(val.c_str(), &end, 10);
       ok = end != val.c_str() && x > 0 && x <= (1 << 15);
       (name == "width" ? width : name == "height" ? height : spp) = (int)x;
+    } else if (name == "depth") {
+      char* end = nullptr;
+      const long x = std::strtol(val.c_str(), &end, 10);
+      ok = end != val.c_str() && *end == '\0' && x >= 0 && x <= CRT_MAX_DEPTH;
+      depth = (int)x;
     } else if (name == "fstop") {
       ok = scalar(val, cam.fstop);
     } else if (name == "fov") {
@@ -172,7 +182,14 @@ int main(int argc, char** argv) {
   crt_render_params params{width, height, spp, 0, 0};
   crt_render_out out{};
   out.rgb8 = rgb.data();
-  if (crt_render(scene, &cam, &light, &params, &out, nullptr) != CRT_OK) return die("rendering");
+  if (depth == 0) {
+    if (crt_render(scene, &cam, &light, &params, &out, nullptr) != CRT_OK) return die("rendering");
+  } else {
+    std::vector<crt_optics> optics((size_t)desc.num_materials);
+    crt_obj_optics(obj, optics.data());
+    if (crt_render_recursive(scene, &cam, &light, &params, depth, optics.data(), &out, nullptr) != CRT_OK)
+      return die("rendering");
+  }
   if (crt_scene_check(scene, nullptr) != CRT_OK) return die("rendering");
   if (!output.empty() && crt_write_bmp(output.c_str(), width, height, rgb.data()) != CRT_OK)
     return die("writing the image");

@@ -95,6 +95,7 @@ def lib():
             "crt_trace_closest": [vp, vp, i64, vp, vp, vp, vp],
             "crt_trace_shadow": [vp, vp, i64, vp, vp, vp],
             "crt_render": [vp, vp, vp, vp, vp, vp],
+            "crt_render_recursive": [vp, vp, vp, vp, i32, vp, vp, vp],
             "crt_morton": [vp, vp, i32, vp, vp, vp],
             "crt_sort_pairs": [vp, vp, vp, vp, i32, i32, vp],
             "crt_sort_pairs_noalloc": [vp, vp, vp, vp, i32, i32, vp],
@@ -110,6 +111,7 @@ def lib():
             "crt_batch_check": [vp, vp],
             "crt_obj_load": [C.c_char_p, C.c_char_p, vp],
             "crt_obj_mesh": [vp, vp],
+            "crt_obj_optics": [vp, vp],
             "crt_obj_free": [vp],
             "crt_write_bmp": [C.c_char_p, i32, i32, vp],
         }
@@ -271,6 +273,26 @@ class Scene:
         return out
 
 
+    def render_recursive(self, camera, light, width, height, spp, depth, optics=None, rows=None, rays=False,
+                         stream=None):
+        """crt_render_recursive: traceRay with `depth` levels of reflected and
+        refracted rays.  optics: (num_materials, 4) array of kr xyz and ior,
+        or None (kr = ks, ior = 1).  Returns rgb8, rgb_f64, the primary hit_id
+        and hit_t, and (rays=True) the primary rays."""
+        cam, lt, p = render_args(camera, light, width, height, spp, rows)
+        npx, ns = width * height, width * height * spp
+        out = dict(rgb8=np.zeros((npx, 3), np.uint8), rgb_f64=np.zeros((npx, 3), np.float64),
+                   hit_id=np.zeros(ns, np.int32), hit_t=np.zeros(ns, np.float64))
+        if rays:
+            out["rays"] = np.zeros((ns, 6), np.float64)
+        op = None if optics is None else np.ascontiguousarray(optics, np.float64).reshape(-1, 4)
+        o = _RenderOut(*[_addr(out.get(k)) for k in ("rgb8", "rgb_f32", "hit_id", "hit_t", "shadow", "rays",
+                                                     "traversal_stats", "rgb_f64", "depth", "shadow_id")])
+        _check(lib().crt_render_recursive(self.h, C.byref(cam), C.byref(lt), C.byref(p), int(depth), _addr(op),
+                                          C.byref(o), _stream(stream)))
+        return out
+
+
 class Batch:
     """Many meshes, each with its own camera, light and image size, built and
     rendered together (crt_batch_*).  `meshes` are data.Mesh objects, `views`
@@ -352,8 +374,10 @@ class Batch:
         return out
 
 
-def load_obj_native(path, mtl_dir=None):
-    """crt_obj_load: the library's OBJ/MTL reader (host only), as a data.Mesh."""
+def load_obj_native(path, mtl_dir=None, with_optics=False):
+    """crt_obj_load: the library's OBJ/MTL reader (host only), as a data.Mesh;
+    with_optics also returns crt_obj_optics as a (num_materials, 4) array of
+    kr xyz (= Ks) and ior (= Ni)."""
     from .data import Mesh
     h = C.c_void_p()
     _check(lib().crt_obj_load(os.fsencode(path), None if mtl_dir is None else os.fsencode(mtl_dir), C.byref(h)))
@@ -367,12 +391,15 @@ def load_obj_native(path, mtl_dir=None):
             return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ct)), (n,)).astype(dt).reshape(shape)
 
         n, nv, nn, nm = d.num_triangles, d.num_vertices, d.num_normals, d.num_materials
-        return Mesh(arr(d.vertices, 3 * nv, C.c_float, np.float32, (nv, 3)),
+        optics = np.zeros((nm, 4), np.float64)
+        _check(lib().crt_obj_optics(h, optics.ctypes.data))
+        mesh = Mesh(arr(d.vertices, 3 * nv, C.c_float, np.float32, (nv, 3)),
                     arr(d.vertex_indices, 3 * n, C.c_int32, np.int32, (n, 3)),
                     arr(d.normals, 3 * nn, C.c_float, np.float32, (nn, 3)),
                     arr(d.normal_indices, 3 * n, C.c_int32, np.int32, (n, 3)),
                     arr(d.material_ids, n, C.c_int32, np.int32, (n,)),
                     arr(d.materials, 16 * nm, C.c_double, np.float64, (nm, 16)))
+        return (mesh, optics) if with_optics else mesh
     finally:
         lib().crt_obj_free(h)
 

@@ -387,22 +387,20 @@ crt_status crt_trace_shadow(crt_scene* s, const double* rays, int64_t n, int32_t
   return trace_common(s, rays, n, ids, t, nullptr, true, stream);
 }
 
-crt_status crt_render(crt_scene* s, const crt_camera* cam, const crt_light* light, const crt_render_params* p,
-                      const crt_render_out* o, void* stream) {
-  if (!s || !cam || !light || !p || !o) return fail(CRT_INVALID_ARG, "null argument");
+// The checks and the RenderArgs shared by crt_render, crt_render_recursive
+// and crt_adjoint_lambert (the constants of raytracer.cu:126-130, 144; tan on
+// the host).  Outputs start unset.
+static crt_status render_args(crt_scene* s, const crt_camera* cam, const crt_light* light,
+                              const crt_render_params* p, RenderArgs& a) {
   if (!s->built) return fail(CRT_NOT_BUILT, "no BVH");
   if (p->width <= 0 || p->height <= 0 || p->spp <= 0) return fail(CRT_INVALID_ARG, "width, height, spp must be > 0");
   if ((int64_t)p->width * p->height > (int64_t)1 << 30) return fail(CRT_INVALID_ARG, "image too large");
   int row0 = p->row_begin, row1 = p->row_end;
   if (row0 == 0 && row1 == 0) row1 = p->height;
   if (row0 < 0 || row1 > p->height || row0 >= row1) return fail(CRT_INVALID_ARG, "bad row range");
-  cudaStream_t st = S(stream);
-  const size_t npx = (size_t)p->width * p->height;
-  const size_t nsm = npx * (size_t)p->spp;
-  RenderArgs a;
+  a = RenderArgs{};
   a.W = p->width, a.H = p->height, a.spp = p->spp, a.row0 = row0, a.row1 = row1;
   a.group = lanes_per_pixel(p->spp, kDefaultLanesPerPixel);
-  // the constants of raytracer.cu:126-130, 144; tan on the host
   a.angle = std::tan(M_PI * 0.5 * cam->fov / 180.0f);
   a.aspect = double(p->width) / double(p->height);
   a.invW = 1.0 / double(p->width);
@@ -417,9 +415,20 @@ crt_status crt_render(crt_scene* s, const crt_camera* cam, const crt_light* ligh
   a.lradius = light->radius;
   a.latt[0] = light->constant_term, a.latt[1] = light->linear_term, a.latt[2] = light->quadratic_term;
   a.counter = s->counter;
+  return CRT_OK;
+}
+
+crt_status crt_render(crt_scene* s, const crt_camera* cam, const crt_light* light, const crt_render_params* p,
+                      const crt_render_out* o, void* stream) {
+  if (!s || !cam || !light || !p || !o) return fail(CRT_INVALID_ARG, "null argument");
+  RenderArgs a;
+  if (crt_status e = render_args(s, cam, light, p, a)) return e;
+  cudaStream_t st = S(stream);
+  const size_t npx = (size_t)p->width * p->height;
+  const size_t nsm = npx * (size_t)p->spp;
   // outputs: whole-image buffers; a row band writes only its rows
   DevView v8, vf, vh, vt, vs, vr, vst, vd, vdp, vsi;
-  const bool band = !(row0 == 0 && row1 == p->height);
+  const bool band = !(a.row0 == 0 && a.row1 == p->height);
   CRT_CUDA(v8.open(o->rgb8, 3 * npx, band, st), "stage rgb8");
   CRT_CUDA(vf.open(o->rgb_f32, 3 * sizeof(float) * npx, band, st), "stage rgb_f32");
   CRT_CUDA(vh.open(o->hit_id, sizeof(int32_t) * nsm, band, st), "stage hit_id");
@@ -458,6 +467,51 @@ crt_status crt_render(crt_scene* s, const crt_camera* cam, const crt_light* ligh
   return CRT_OK;
 }
 
+crt_status crt_render_recursive(crt_scene* s, const crt_camera* cam, const crt_light* light,
+                                const crt_render_params* p, int32_t depth, const crt_optics* optics,
+                                const crt_render_out* o, void* stream) {
+  if (!s || !cam || !light || !p || !o) return fail(CRT_INVALID_ARG, "null argument");
+  if (depth < 0 || depth > CRT_MAX_DEPTH) return fail(CRT_INVALID_ARG, "depth must be in [0, CRT_MAX_DEPTH]");
+  if (o->traversal_stats || o->shadow || o->shadow_id || o->depth)
+    return fail(CRT_INVALID_ARG, "crt_render_recursive writes rgb8, rgb_f32, rgb_f64, hit_id, hit_t and rays only");
+  RenderArgs a;
+  if (crt_status e = render_args(s, cam, light, p, a)) return e;
+  cudaStream_t st = S(stream);
+  // kr and ior per material (host or device array); NULL: the kernel takes
+  // kr = ks and ior = 1
+  static_assert(sizeof(DOptics) == sizeof(crt_optics) && kMaxRecDepth == CRT_MAX_DEPTH, "crt_optics layout");
+  DevView vo;
+  CRT_CUDA(vo.open(const_cast<crt_optics*>(optics), sizeof(DOptics) * (size_t)s->m.nmat, true, st), "stage optics");
+  const size_t npx = (size_t)p->width * p->height;
+  const size_t nsm = npx * (size_t)p->spp;
+  const bool band = !(a.row0 == 0 && a.row1 == p->height);
+  DevView v8, vf, vh, vt, vr, vd;
+  CRT_CUDA(v8.open(o->rgb8, 3 * npx, band, st), "stage rgb8");
+  CRT_CUDA(vf.open(o->rgb_f32, 3 * sizeof(float) * npx, band, st), "stage rgb_f32");
+  CRT_CUDA(vh.open(o->hit_id, sizeof(int32_t) * nsm, band, st), "stage hit_id");
+  CRT_CUDA(vt.open(o->hit_t, sizeof(double) * nsm, band, st), "stage hit_t");
+  CRT_CUDA(vr.open(o->rays, 6 * sizeof(double) * nsm, band, st), "stage rays");
+  CRT_CUDA(vd.open(o->rgb_f64, 3 * sizeof(double) * npx, band, st), "stage rgb_f64");
+  a.rgb8 = static_cast<uint8_t*>(v8.dev);
+  a.rgbf = static_cast<float*>(vf.dev);
+  a.hit_id = static_cast<int*>(vh.dev);
+  a.hit_t = static_cast<double*>(vt.dev);
+  a.rays = static_cast<double*>(vr.dev);
+  a.rgbd = static_cast<double*>(vd.dev);
+  CRT_CUDA(launch_render_recursive(dscene(s), a, static_cast<const DOptics*>(vo.dev), depth, st),
+           "recursive render launch");
+  CRT_CUDA(vo.close(false, st), "unstage");
+  const bool host_out = v8.temp || vf.temp || vh.temp || vt.temp || vr.temp || vd.temp;
+  CRT_CUDA(v8.close(true, st), "unstage");
+  CRT_CUDA(vf.close(true, st), "unstage");
+  CRT_CUDA(vh.close(true, st), "unstage");
+  CRT_CUDA(vt.close(true, st), "unstage");
+  CRT_CUDA(vr.close(true, st), "unstage");
+  CRT_CUDA(vd.close(true, st), "unstage");
+  if (host_out) return check_globals(s, st);
+  return CRT_OK;
+}
+
 crt_status crt_scene_set_materials(crt_scene* s, const crt_material* mats, int32_t num, void* stream) {
   if (!s || !mats) return fail(CRT_INVALID_ARG, "null argument");
   if (num != s->m.nmat) return fail(CRT_INVALID_ARG, "material count differs from the scene's");
@@ -469,33 +523,10 @@ crt_status crt_adjoint_lambert(crt_scene* s, const crt_camera* cam, const crt_li
                                const crt_render_params* p, const double* grad_rgb, const double* grad_depth,
                                double* grad_vertices, double* grad_light, double* grad_kd, void* stream) {
   if (!s || !cam || !light || !p || !grad_rgb) return fail(CRT_INVALID_ARG, "null argument");
-  if (!s->built) return fail(CRT_NOT_BUILT, "no BVH");
-  if (p->width <= 0 || p->height <= 0 || p->spp <= 0) return fail(CRT_INVALID_ARG, "width, height, spp must be > 0");
-  if ((int64_t)p->width * p->height > (int64_t)1 << 30) return fail(CRT_INVALID_ARG, "image too large");
-  int row0 = p->row_begin, row1 = p->row_end;
-  if (row0 == 0 && row1 == 0) row1 = p->height;
-  if (row0 < 0 || row1 > p->height || row0 >= row1) return fail(CRT_INVALID_ARG, "bad row range");
+  RenderArgs a;
+  if (crt_status e = render_args(s, cam, light, p, a)) return e;
   cudaStream_t st = S(stream);
   const size_t npx = (size_t)p->width * p->height;
-  RenderArgs a;
-  a.W = p->width, a.H = p->height, a.spp = p->spp, a.row0 = row0, a.row1 = row1;
-  a.group = lanes_per_pixel(p->spp, kDefaultLanesPerPixel);
-  a.angle = std::tan(M_PI * 0.5 * cam->fov / 180.0f);
-  a.aspect = double(p->width) / double(p->height);
-  a.invW = 1.0 / double(p->width);
-  a.invH = 1.0 / double(p->height);
-  a.aperture = 1 / cam->fstop;
-  a.focal = cam->focal_point;
-  for (int k = 0; k < 3; k++) {
-    a.eye[k] = cam->eye[k];
-    a.lpos[k] = light->position[k];
-    a.lcol[k] = light->color[k];
-  }
-  a.lradius = light->radius;
-  a.latt[0] = light->constant_term, a.latt[1] = light->linear_term, a.latt[2] = light->quadratic_term;
-  a.counter = s->counter;
-  a.rgb8 = nullptr, a.rgbf = nullptr, a.hit_id = nullptr, a.hit_t = nullptr, a.shadow = nullptr, a.rays = nullptr;
-  a.stats = nullptr;
   DevView vg, vgd;
   CRT_CUDA(vg.open(const_cast<double*>(grad_rgb), 3 * sizeof(double) * npx, true, st), "stage grad_rgb");
   CRT_CUDA(vgd.open(const_cast<double*>(grad_depth), sizeof(double) * npx, true, st), "stage grad_depth");

@@ -116,6 +116,17 @@ struct RenderArgs {
 };
 cudaError_t launch_render(const DScene& S, const RenderArgs& a, cudaStream_t st);
 
+// recursive.cu: traceRay with reflected and refracted rays, at most
+// kMaxRecDepth levels below the primary ray.  optics[m] (device, may be
+// NULL): kr and ior of material m.
+constexpr int kMaxRecDepth = 8;
+struct DOptics {
+  double kr[3];
+  double ior;
+};
+cudaError_t launch_render_recursive(const DScene& S, const RenderArgs& a, const DOptics* optics, int depth,
+                                    cudaStream_t st);
+
 // Device view of a batch for the batched pixel kernel.
 struct BatchView {
   int M = 0, items = 0;

@@ -8,8 +8,8 @@
 // (1-based or negative indices), polygons fan-triangulated (0, k, k+1),
 // "mtllib" (read from mtl_dir, or the OBJ's directory), "usemtl" (unknown
 // or absent names give material 0).  Coordinates are rounded to FP32, the
-// precision of crt_mesh_desc.  MTL: newmtl, Ka, Kd, Ks, Kt/Tf, Ke, Ns
-// (tinyobjloader's defaults: colours 0, shininess 1).  A missing MTL file
+// precision of crt_mesh_desc.  MTL: newmtl, Ka, Kd, Ks, Kt/Tf, Ke, Ns, Ni
+// (tinyobjloader's defaults: colours 0, shininess 1, ior 1).  A missing MTL file
 // is skipped, as tinyobjloader warns and goes on; a mesh without materials
 // gets one Lambert material (kd 0.8).  Every face corner must name a normal:
 // the reference reads normals[-1] otherwise, so such files are rejected.
@@ -34,6 +34,7 @@ struct crt_obj {
   std::vector<float> v, n;
   std::vector<int32_t> vi, ni, mid;
   std::vector<crt_material> mats;
+  std::vector<double> ior;  // per material: MTL Ni
 };
 
 namespace {
@@ -71,7 +72,8 @@ std::string dir_of(const std::string& path) {
   return k == std::string::npos ? std::string() : path.substr(0, k + 1);
 }
 
-void read_mtl(const std::string& file, std::map<std::string, int>& names, std::vector<crt_material>& mats) {
+void read_mtl(const std::string& file, std::map<std::string, int>& names, std::vector<crt_material>& mats,
+              std::vector<double>& ior) {
   std::ifstream f(file);
   if (!f) return;  // tinyobjloader warns and goes on
   std::string line;
@@ -85,6 +87,7 @@ void read_mtl(const std::string& file, std::map<std::string, int>& names, std::v
       z.shininess = 1.0;
       names[t[1]] = (int)mats.size();
       mats.push_back(z);
+      ior.push_back(1.0);
       m = &mats.back();
       continue;
     }
@@ -101,6 +104,9 @@ void read_mtl(const std::string& file, std::map<std::string, int>& names, std::v
     } else if (t[0] == "Ns" && t.size() >= 2) {
       double s;
       if (parse_double(t[1], s)) m->shininess = s;
+    } else if (t[0] == "Ni" && t.size() >= 2) {
+      double s;
+      if (parse_double(t[1], s)) ior.back() = s;
     }
   }
 }
@@ -157,7 +163,7 @@ crt_status crt_obj_load(const char* obj_path, const char* mtl_dir, crt_obj** out
     } else if (t[0] == "mtllib" && t.size() >= 2) {
       std::string p = base;
       if (!p.empty() && p.back() != '/') p += '/';
-      read_mtl(p + t[1], names, o->mats);
+      read_mtl(p + t[1], names, o->mats, o->ior);
     } else if (t[0] == "usemtl") {
       const auto it = t.size() >= 2 ? names.find(t[1]) : names.end();
       cur = it == names.end() ? -1 : it->second;
@@ -189,6 +195,7 @@ crt_status crt_obj_load(const char* obj_path, const char* mtl_dir, crt_obj** out
     std::memset(&z, 0, sizeof(z));
     z.kd[0] = z.kd[1] = z.kd[2] = 0.8;
     o->mats.push_back(z);
+    o->ior.push_back(1.0);
   }
   for (int32_t& m : o->mid)
     if (m < 0) m = 0;
@@ -214,6 +221,15 @@ crt_status crt_obj_mesh(const crt_obj* o, crt_mesh_desc* mesh) {
   mesh->materials = o->mats.data();
   mesh->num_materials = (int32_t)o->mats.size();
   mesh->material_ids = o->mid.data();
+  return CRT_OK;
+}
+
+crt_status crt_obj_optics(const crt_obj* o, crt_optics* optics) {
+  if (!o || !optics) return fail("null argument");
+  for (size_t m = 0; m < o->mats.size(); m++) {
+    for (int k = 0; k < 3; k++) optics[m].kr[k] = o->mats[m].ks[k];  // mat.kr = specular, src/scene.cpp:29
+    optics[m].ior = o->ior[m];
+  }
   return CRT_OK;
 }
 

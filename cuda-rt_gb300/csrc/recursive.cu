@@ -1,0 +1,285 @@
+// recursive.cu -- traceRay with reflected and refracted rays on sm_103a.
+//
+// The reference's traceRay (kernels/raytracer.cu:169-249) takes a depth and
+// carries a Whitted-style reflection/refraction block (raytracer.cu:196-237)
+// that is commented out, so its renders stop at shade().  k_pixels_rec runs
+// that block: below every primary ray, while depth > 0, a reflective
+// material (kr != 0) adds kr % traceRay(reflected ray, depth - 1), then a
+// transmissive one (kt != 0) adds kt % traceRay(refracted ray, depth - 1)
+// unless the refracted ray is totally internally reflected.  As written the
+// block tests Refl()/Trans(), which setBools() defines as isZero(kr) and
+// isZero(kt) (inc/material.h:27-31): it would trace the rays of materials
+// that cannot reflect and add zero.  The kernel follows the evident intent
+// (trace when the coefficient is non-zero).  Secondary rays start at
+// q = r.at(t) with no offset and use the closest-hit search of the primary
+// rays (negative t accepted, |t| < RAY_EPSILON rejected).
+//
+// Every shade() draws three numbers from the pixel's mrand stream, so the
+// stream position of a ray depends on every hit before it in depth-first
+// order, across the pixel's samples too.  One lane therefore owns one pixel
+// and walks its ray tree depth first with an explicit frame stack (at most
+// depth + 1 frames, in local memory); the sums are formed in the recursion's
+// order (shade, + kr % reflected, + kt % refracted), so the colours equal a
+// recursive evaluation bit for bit.  The traversals are warp-synchronous:
+// each step of the loop traces the next ray of every lane that has one, then
+// the shadow rays of the lanes whose ray hit.
+#include "crt_internal.h"
+
+namespace crt {
+
+namespace {
+
+struct Frame {
+  D3 c;        // colour so far: shade(), then each child's contribution
+  D3 q, N, d;  // hit point, smooth normal, incoming direction
+  int mid;     // material
+  int stage;   // 0 no child yet, 1 reflected child out, 2 refracted child out, 3 done
+};
+
+__device__ __forceinline__ bool nonzero3(const double* k) { return !(k[0] == 0 && k[1] == 0 && k[2] == 0); }
+
+// kr and ior of material m: the caller's table, or (optics NULL) kr = ks, as
+// Scene_h::LoadObj sets it (src/scene.cpp:29), and tinyobjloader's ior of 1.
+__device__ __forceinline__ const double* kr_of(const DOptics* optics, const DMat* mats, int m) {
+  return optics ? optics[m].kr : mats[m].ks;
+}
+__device__ __forceinline__ double ior_of(const DOptics* optics, int m) { return optics ? optics[m].ior : 1.0; }
+
+// The next child ray of frame f (the commented block's order: reflection,
+// then refraction), or false when f has no more children.
+__device__ bool next_child(Frame& f, const DOptics* __restrict__ optics, const DMat* __restrict__ mats, D3& org,
+                           D3& dir) {
+  if (f.stage == 0) {
+    f.stage = 1;
+    if (nonzero3(kr_of(optics, mats, f.mid))) {
+      // Rdir = -2.0*(r.getDirection()*i.N)*i.N + r.getDirection(); normalize
+      dir = normalize_exact((-2.0 * dot(f.d, f.N)) * f.N + f.d);
+      org = f.q;
+      return true;
+    }
+  }
+  if (f.stage == 1) {
+    f.stage = 3;
+    if (nonzero3(mats[f.mid].kt)) {
+      D3 n = f.N;
+      const D3 rd = f.d;
+      const D3 rcos = dot(d3(-rd.x, -rd.y, -rd.z), n) * n;  // n*(-rd*n)
+      const D3 rsin = rcos + rd;
+      const double etai = 1.0, etat = ior_of(optics, f.mid);
+      double eta;
+      if (dot(rd, n) < 0) {
+        eta = etai / etat;
+        n = d3(-n.x, -n.y, -n.z);
+      } else {
+        eta = etat / etai;
+      }
+      const D3 tsin = eta * rsin;
+      const double TIR = 1 - dot(tsin, tsin);
+      if (TIR >= 0) {
+        const D3 tcos = sqrt(TIR) * n;
+        dir = normalize_exact(tcos + tsin);
+        org = f.q;
+        f.stage = 2;
+        return true;
+      }
+    }
+  }
+  f.stage = 3;
+  return false;
+}
+
+// A child's colour v returns to its parent frame f.
+__device__ __forceinline__ void add_child(Frame& f, const DOptics* __restrict__ optics,
+                                          const DMat* __restrict__ mats, D3 v) {
+  const double* k = f.stage == 1 ? kr_of(optics, mats, f.mid) : mats[f.mid].kt;
+  f.c = f.c + d3(k[0] * v.x, k[1] * v.y, k[2] * v.z);
+}
+
+struct PixelRay {
+  D3 org, dir;
+};
+
+// Primary ray of the next sample: two draws (lens angle and radius), the
+// thin-lens ray of runRayTracerKernelRec (raytracer.cu:141-152).
+__device__ __forceinline__ PixelRay primary(const RenderArgs& A, D3 fdir, uint32_t& st) {
+  const double dofAngle = 2 * 3.14159265358979323846 * rand_double(st);
+  const double dofRadius = A.aperture * sqrt(rand_double(st)) / 2.0;
+  D3 org = d3(0.0, 0.0, 0.0);
+  if (dofRadius != 0.0) {
+    double sa, ca;
+    sincos(dofAngle, &sa, &ca);
+    org = d3(dofRadius * ca, dofRadius * sa, 0.0);
+  }
+  return PixelRay{org, normalize_exact(fdir - org)};
+}
+
+__global__ void __launch_bounds__(128) k_pixels_rec(DScene S, RenderArgs A, const DOptics* __restrict__ optics,
+                                                    int depth) {
+  const unsigned full = 0xffffffffu;
+  float rb[6], B, D;
+  scene_consts(S, rb, B, D);
+  const int lane = threadIdx.x & 31;
+  const int tiles_x = (A.W + 7) / 8, tiles_y = (A.row1 - A.row0 + 3) / 4;
+  const int ntiles = tiles_x * tiles_y;
+  const int gx = (A.W + 15) / 16;
+  const D3 lpos = d3(A.lpos[0], A.lpos[1], A.lpos[2]);
+  Frame fr[kMaxRecDepth];
+  while (true) {
+    int tile = 0;
+    if (lane == 0) tile = (int)atomicAdd(A.counter, 1u);
+    tile = __shfl_sync(full, tile, 0);
+    if (tile >= ntiles) break;
+    const int px = (tile % tiles_x) * 8 + (lane & 7);
+    const int py = A.row0 + (tile / tiles_x) * 4 + (lane >> 3);
+    const bool valid = px < A.W && py < A.row1;
+    const int idx = (A.H - py - 1) * A.W + px;
+    uint32_t st = wang_hash((uint32_t)(((py / 16) * gx + px / 16) * 256 + (py % 16) * 16 + (px % 16)));
+    const double xx = (2 * ((px + 0.5) * A.invW) - 1) * A.angle * A.aspect;
+    const double yy = (1 - 2 * ((py + 0.5) * A.invH)) * A.angle;
+    D3 fdir = normalize_exact(d3(xx, yy, -1.0));
+    fdir = d3(fdir.x * A.focal, fdir.y * A.focal, fdir.z * A.focal);
+    D3 acc = d3(0, 0, 0);
+    int k = 0, lvl = 0;
+    bool busy = valid && A.spp > 0;
+    PixelRay ray{d3(0, 0, 0), d3(0, 0, 1)};
+    if (busy) ray = primary(A, fdir, st);
+    if (busy && A.rays) {
+      double* r = A.rays + 6 * (int64_t)idx * A.spp;
+      r[0] = ray.org.x, r[1] = ray.org.y, r[2] = ray.org.z, r[3] = ray.dir.x, r[4] = ray.dir.y, r[5] = ray.dir.z;
+    }
+    while (__any_sync(full, busy)) {
+      RayC rc;
+      if (busy)
+        ray_setup(rc, ray.org.x, ray.org.y, ray.org.z, ray.dir.x, ray.dir.y, ray.dir.z, B, D);
+      else
+        ray_setup(rc, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0, B, D);
+      HitRec h;
+      const int res = traverse<false>(S, rc, rb, h, busy);
+      if (res < 0) atomicOr(&S.g->err, kErrStack);
+      const bool hit = busy && res > 0;
+      if (busy && lvl == 0) {
+        const int64_t si = (int64_t)idx * A.spp + k;
+        if (A.hit_id) A.hit_id[si] = hit ? h.id : -1;
+        if (A.hit_t) A.hit_t[si] = hit ? h.t : 0.0;
+      }
+      // Light::getDirection (three draws) and the shadow ray of each hit
+      D3 q = d3(0, 0, 0), L = d3(0, 0, 1);
+      double dist = 0.0;
+      RayC sr;
+      if (hit) {
+        q = ray.org + (h.t * ray.dir);
+        const double r0 = rand_double(st), r1 = rand_double(st), r2 = rand_double(st);
+        const D3 off = d3(r0 * A.lradius - 0.5, r1 * A.lradius - 0.5, r2 * A.lradius - 0.5);
+        L = normalize_exact(lpos + off - q);
+        dist = norm_exact(lpos - q);
+        ray_setup(sr, q.x, q.y, q.z, L.x, L.y, L.z, B, D);
+      } else {
+        ray_setup(sr, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0, B, D);
+      }
+      HitRec s;
+      const int sres = traverse<true>(S, sr, rb, s, hit);
+      if (sres < 0) atomicOr(&S.g->err, kErrStack);
+      if (!busy) continue;
+      // Material::shade (kernels/material.cu:6-40), as the plain pixel kernel
+      D3 v = d3(0.9, 0.9, 0.9);
+      D3 N = d3(0, 0, 0);
+      int mid = 0;
+      if (hit) {
+        N = hit_normal(S, h);
+        mid = __ldg(S.matid + h.id);
+        const DMat& m = S.mats[mid];
+        D3 I = d3(m.ke[0] + m.ka[0] * 0.0, m.ke[1] + m.ka[1] * 0.0, m.ke[2] + m.ka[2] * 0.0);
+        D3 V = d3(A.eye[0], A.eye[1], A.eye[2]) - q;
+        V = normalize_exact(d3(-V.x, -V.y, -V.z));
+        double fall = A.latt[0] + (A.latt[1] + A.latt[2] * dist) * dist;
+        fall = fabs(fall) < kRayEps ? 1.0 : 1.0 / fall;
+        const double datt = fmin(1.0, fall);
+        D3 satt = d3(1, 1, 1);
+        if (sres > 0 && s.t < dist && !(s.t < kRayEps)) {
+          const DMat& om = S.mats[__ldg(S.matid + s.id)];
+          const bool otrans = om.kt[0] == 0 && om.kt[1] == 0 && om.kt[2] == 0;  // Trans() = isZero(kt)
+          satt = otrans ? d3(om.kd[0] * (1 - om.kt[0]), om.kd[1] * (1 - om.kt[1]), om.kd[2] * (1 - om.kt[2]))
+                        : d3(0, 0, 0);
+        }
+        const D3 att = datt * satt;
+        double lam = dot(N, L);
+        if (lam < 0) lam = 0;
+        const D3 diffuse = d3(m.kd[0] * lam, m.kd[1] * lam, m.kd[2] * lam);
+        const D3 R = normalize_exact((-2.0 * dot(L, N)) * N + L);
+        double sp = dot(R, V);
+        sp = (double)powf(__double2float_rn(fmax(0.0, sp)), __double2float_rn(m.shininess));
+        const D3 ds = diffuse + d3(m.ks[0] * sp, m.ks[1] * sp, m.ks[2] * sp);
+        v = I + d3(att.x * ds.x * A.lcol[0], att.y * ds.y * A.lcol[1], att.z * ds.z * A.lcol[2]);
+      }
+      // depth-first walk: descend into this ray's first child, or return its
+      // colour up the frames until one has another child or the sample ends
+      if (hit && lvl < depth) {
+        Frame& f = fr[lvl];
+        f.c = v, f.q = q, f.N = N, f.d = ray.dir, f.mid = mid, f.stage = 0;
+        if (next_child(f, optics, S.mats, ray.org, ray.dir)) {
+          lvl++;
+          continue;
+        }
+        v = f.c;
+      }
+      while (true) {
+        if (lvl == 0) {
+          acc = acc + v;
+          if (++k < A.spp) {
+            ray = primary(A, fdir, st);
+            if (A.rays) {
+              double* r = A.rays + 6 * ((int64_t)idx * A.spp + k);
+              r[0] = ray.org.x, r[1] = ray.org.y, r[2] = ray.org.z;
+              r[3] = ray.dir.x, r[4] = ray.dir.y, r[5] = ray.dir.z;
+            }
+          } else {
+            busy = false;
+          }
+          break;
+        }
+        Frame& f = fr[lvl - 1];
+        add_child(f, optics, S.mats, v);
+        if (next_child(f, optics, S.mats, ray.org, ray.dir)) break;
+        v = f.c;
+        lvl--;
+      }
+    }
+    if (!valid || A.spp <= 0) continue;
+    const double inv = (double)A.spp;
+    acc = d3(acc.x / inv, acc.y / inv, acc.z / inv);
+    if (A.rgbf) {
+      A.rgbf[3 * (int64_t)idx] = (float)acc.x;
+      A.rgbf[3 * (int64_t)idx + 1] = (float)acc.y;
+      A.rgbf[3 * (int64_t)idx + 2] = (float)acc.z;
+    }
+    if (A.rgbd) {
+      A.rgbd[3 * (int64_t)idx] = acc.x;
+      A.rgbd[3 * (int64_t)idx + 1] = acc.y;
+      A.rgbd[3 * (int64_t)idx + 2] = acc.z;
+    }
+    if (A.rgb8) {
+      const double cc[3] = {acc.x, acc.y, acc.z};
+#pragma unroll
+      for (int ch = 0; ch < 3; ch++) {
+        double c = cc[ch];
+        if (c < 0) c = 0.0;
+        if (c > 1) c = 1.0;
+        A.rgb8[3 * (int64_t)idx + ch] = (uint8_t)(255.0 * c);
+      }
+    }
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_render_recursive(const DScene& S, const RenderArgs& a, const DOptics* optics, int depth,
+                                    cudaStream_t st) {
+  if (depth < 0 || depth > kMaxRecDepth) return cudaErrorInvalidValue;
+  cudaMemsetAsync(a.counter, 0, sizeof(unsigned), st);
+  int bps = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_pixels_rec, 128, 0);
+  k_pixels_rec<<<num_sms() * (bps > 0 ? bps : 1), 128, 0, st>>>(S, a, optics, depth);
+  return cudaGetLastError();
+}
+
+}  // namespace crt

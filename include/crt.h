@@ -155,6 +155,32 @@ crt_status crt_trace_shadow(crt_scene* scene, const double* rays, int64_t n, int
 crt_status crt_render(crt_scene* scene, const crt_camera* camera, const crt_light* light,
                       const crt_render_params* params, const crt_render_out* out, void* stream);
 
+/* ---- recursive render: traceRay with the reflection and refraction block
+ * of kernels/raytracer.cu:196-237 (commented out in the reference, whose
+ * renders therefore stop at shade()).  Below each primary ray, while depth
+ * > 0, a material with kr != 0 adds kr % (the colour of the mirrored ray)
+ * and then one with kt != 0 adds kt % (the colour of the refracted ray,
+ * Snell's law with eta = 1/ior entering and ior leaving; none on total
+ * internal reflection), each traced with depth - 1.  Secondary rays start
+ * at the hit point with no offset and use crt_render's closest hit and
+ * shade(); every shade() takes its three light draws from the pixel's mrand
+ * stream in depth-first order.  The block's Refl()/Trans() tests are
+ * isZero(kr)/isZero(kt) (inc/material.h:27-31), which would trace only
+ * rays that add nothing; the intent (non-zero coefficient) is followed.
+ * depth = 0 gives crt_render's image.  optics: num_materials entries (host
+ * or device), or NULL for kr = ks (as Scene_h::LoadObj sets it,
+ * src/scene.cpp:29) and ior = 1 (tinyobjloader's default).  Writes rgb8,
+ * rgb_f32, rgb_f64, and the primary rays' hit_id, hit_t and rays; the
+ * other outputs must be NULL. */
+#define CRT_MAX_DEPTH 8
+typedef struct crt_optics {
+  double kr[3]; /* Material::kr, inc/material.h:16 */
+  double ior;   /* Material::ior (MTL Ni) */
+} crt_optics;
+crt_status crt_render_recursive(crt_scene* scene, const crt_camera* camera, const crt_light* light,
+                                const crt_render_params* params, int32_t depth, const crt_optics* optics,
+                                const crt_render_out* out, void* stream);
+
 /* Replace the material table (same count as at creation), e.g. new
  * per-triangle albedos.  Asynchronous. */
 crt_status crt_scene_set_materials(crt_scene* scene, const crt_material* materials, int32_t num_materials,
@@ -272,6 +298,10 @@ crt_status crt_batch_check(crt_batch* batch, void* stream);
 typedef struct crt_obj crt_obj;
 crt_status crt_obj_load(const char* obj_path, const char* mtl_dir, crt_obj** out);
 crt_status crt_obj_mesh(const crt_obj* obj, crt_mesh_desc* mesh);
+/* crt_obj_optics fills one crt_optics per material (crt_mesh_desc's
+ * num_materials) for crt_render_recursive: kr = Ks, as Scene_h::LoadObj sets
+ * it (src/scene.cpp:29), and ior = Ni (default 1). */
+crt_status crt_obj_optics(const crt_obj* obj, crt_optics* optics);
 crt_status crt_obj_free(crt_obj* obj);
 /* writeBMP (src/bitmap.cpp:99-154): 24-bit BMP of a host rgb8 image in
  * crt_render_out's bottom-up order (rows padded to 4 bytes with zeros). */

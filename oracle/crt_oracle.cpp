@@ -413,6 +413,128 @@ struct orc_light {  // Light_h, inc/Light.h:7-29 (positional light)
   double constant_term, linear_term, quadratic_term;
 };
 
+// Material::shade (kernels/material.cu:6-40) at the closest hit hh of the ray
+// (org, dir), N its smooth normal, with the positional Light: getDirection
+// takes three draws from st (Light.cu:71-80), distanceAttenuation
+// (Light.cu:56-68), shadowAttenuation from q = r.at(t) with no offset
+// (Light.cu:5-37).  *sh: 1 occluded, 0 lit; *shid: the occluder or -1;
+// *overflow counts stack overflows of the shadow ray.
+static V3 shade_hit(const Scene& s, const orc_camera* cam, const orc_light* light, V3 org, V3 dir, const Hit& hh,
+                    V3 N, uint32_t& st, int* sh, int* shid, int* overflow) {
+  const V3 lpos = v3(light->position[0], light->position[1], light->position[2]);
+  const V3 lcol = v3(light->color[0], light->color[1], light->color[2]);
+  const V3 eye = v3(cam->eye[0], cam->eye[1], cam->eye[2]);
+  V3 q = org + (hh.t * dir);
+  const Material& m = s.mats[s.matid[hh.id]];
+  V3 I = v3(m.ke[0] + m.ka[0] * 0.0, m.ke[1] + m.ka[1] * 0.0, m.ke[2] + m.ka[2] * 0.0);
+  V3 Vv = eye - q;
+  Vv = v3(-Vv.x, -Vv.y, -Vv.z);
+  Vv = normalize(Vv);
+  double r0 = rand_double(st);
+  double r1 = rand_double(st);
+  double r2 = rand_double(st);
+  V3 off = v3(r0, r1, r2) * light->radius;
+  off = v3(off.x - 0.5, off.y - 0.5, off.z - 0.5);
+  V3 L = normalize(lpos + off - q);
+  double dist = norm(lpos - q);
+  double fall = light->constant_term + (light->linear_term + light->quadratic_term * dist) * dist;
+  fall = (fabs(fall) < kRayEps) ? 1.0 : 1.0 / fall;
+  double datt = fmin(1.0, fall);
+  V3 satt = v3(1, 1, 1);
+  Hit sh_hit;
+  int sres = traverse(s, q, L, true, &sh_hit);
+  if (sres < 0) (*overflow)++;
+  *sh = 0;
+  *shid = -1;
+  if (sres > 0 && sh_hit.t < norm(lpos - q)) {
+    const Material& om = s.mats[s.matid[sh_hit.id]];
+    if (sh_hit.t < kRayEps) {
+      satt = v3(1, 1, 1);
+    } else {
+      *sh = 1;
+      *shid = sh_hit.id;
+      // Trans() is isZero(kt) (inc/material.h:31), so an opaque
+      // occluder (kt = 0) passes kd % (1 - kt).
+      bool trans = om.kt[0] == 0 && om.kt[1] == 0 && om.kt[2] == 0;
+      if (trans)
+        satt = v3(om.kd[0] * (1 - om.kt[0]), om.kd[1] * (1 - om.kt[1]), om.kd[2] * (1 - om.kt[2]));
+      else
+        satt = v3(0, 0, 0);
+    }
+  }
+  V3 att = datt * satt;
+  double lam = dot(N, L);
+  if (lam < 0) lam = 0;
+  V3 diffuse = v3(m.kd[0] * lam, m.kd[1] * lam, m.kd[2] * lam);
+  V3 R = (-2.0 * dot(L, N)) * N + L;
+  R = normalize(R);
+  double sp = dot(R, Vv);
+  sp = (double)powf((float)fmax(0.0, sp), (float)m.shininess);
+  V3 spec = v3(m.ks[0] * sp, m.ks[1] * sp, m.ks[2] * sp);
+  return I + mulc(mulc(att, diffuse + spec), lcol);
+}
+
+// traceRay (kernels/raytracer.cu:169-249) with the reflection and refraction
+// block of raytracer.cu:196-237 (commented out in the reference) taking
+// part: after shade(), while depth > 0, a reflective material (kr != 0)
+// adds kr % traceRay(reflected ray, depth - 1), then a transmissive one
+// (kt != 0) adds kt % traceRay(refracted ray, depth - 1) unless the ray is
+// totally internally reflected.  The block tests Refl()/Trans(), which
+// setBools() defines as isZero(kr)/isZero(kt) (inc/material.h:27-31), so
+// as written it would trace the rays of materials that cannot reflect and
+// add nothing; this restatement takes the evident intent (trace when the
+// coefficient is non-zero).  Secondary rays start at q = r.at(t) with no
+// offset and use the same closest-hit search as primary rays (negative t
+// accepted, |t| < RAY_EPSILON rejected).  optics[4*m]: kr xyz, ior of
+// material m.  Draws from st in the recursion's order (depth first).
+static V3 trace_rec(const Scene& s, const orc_camera* cam, const orc_light* light, const double* optics, V3 org,
+                    V3 dir, int depth, uint32_t& st, int* overflow, Hit* first, int* first_res) {
+  Hit hh;
+  int res = traverse(s, org, dir, false, &hh);
+  if (res < 0) (*overflow)++;
+  if (first) *first = hh, *first_res = res;
+  if (res <= 0) return v3(0.9, 0.9, 0.9);
+  const V3 N = hit_normal(s, hh);
+  int sh, shid;
+  V3 c = shade_hit(s, cam, light, org, dir, hh, N, st, &sh, &shid, overflow);
+  if (depth <= 0) return c;
+  const V3 q = org + (hh.t * dir);
+  const int mid = s.matid[hh.id];
+  const Material& m = s.mats[mid];
+  const double* o = optics + 4 * (size_t)mid;
+  if (!(o[0] == 0 && o[1] == 0 && o[2] == 0)) {
+    V3 Rdir = (-2.0 * dot(dir, N)) * N + dir;
+    Rdir = normalize(Rdir);
+    V3 v = trace_rec(s, cam, light, optics, q, Rdir, depth - 1, st, overflow, nullptr, nullptr);
+    c = c + mulc(v3(o[0], o[1], o[2]), v);
+  }
+  if (!(m.kt[0] == 0 && m.kt[1] == 0 && m.kt[2] == 0)) {
+    V3 n = N;
+    const V3 rd = dir;
+    const V3 mrd = v3(-rd.x, -rd.y, -rd.z);
+    const V3 rcos = n * dot(mrd, n);
+    const V3 rsin = rcos + rd;
+    const double etai = 1.0, etat = o[3];
+    double eta;
+    if (dot(rd, n) < 0) {
+      eta = etai / etat;
+      n = v3(-n.x, -n.y, -n.z);
+    } else {
+      eta = etat / etai;
+    }
+    const V3 tsin = eta * rsin;
+    const double TIR = 1 - dot(tsin, tsin);
+    if (TIR >= 0) {
+      const V3 tcos = n * sqrt(TIR);
+      V3 Tdir = tcos + tsin;
+      Tdir = normalize(Tdir);
+      V3 v = trace_rec(s, cam, light, optics, q, Tdir, depth - 1, st, overflow, nullptr, nullptr);
+      c = c + mulc(v3(m.kt[0], m.kt[1], m.kt[2]), v);
+    }
+  }
+  return c;
+}
+
 void* orc_scene_create(int nv, const float* verts, int nn, const float* normals, int ntri,
                        const int* vidx, const int* nidx, int nmat, const orc_material* mats,
                        const int* matid) {
@@ -547,9 +669,6 @@ int orc_render(void* h, const orc_camera* cam, const orc_light* light, int W, in
   const double aspect = double(W) / double(H);
   const double angle = tan(M_PI * 0.5 * cam->fov / 180.0f);  // raytracer.cu:130
   const double aperture = 1 / cam->fstop;  // Camera::getAperature
-  const V3 lpos = v3(light->position[0], light->position[1], light->position[2]);
-  const V3 lcol = v3(light->color[0], light->color[1], light->color[2]);
-  const V3 eye = v3(cam->eye[0], cam->eye[1], cam->eye[2]);
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #pragma omp parallel for collapse(2) schedule(dynamic, 64) reduction(+ : overflow)
@@ -587,64 +706,10 @@ int orc_render(void* h, const orc_camera* cam, const orc_light* light, int W, in
         if (res < 0) overflow++;
         V3 col;
         int sh = -1, shid = -1;
-        if (res > 0) {
-          V3 q = org + (hh.t * dir);
-          const Material& m = s->mats[s->matid[hh.id]];
-          V3 N = hit_normal(*s, hh);
-          // Material::shade, material.cu:6-40
-          V3 I = v3(m.ke[0] + m.ka[0] * 0.0, m.ke[1] + m.ka[1] * 0.0, m.ke[2] + m.ka[2] * 0.0);
-          V3 Vv = eye - q;
-          Vv = v3(-Vv.x, -Vv.y, -Vv.z);
-          Vv = normalize(Vv);
-          // Light::getDirection, Light.cu:71-80: three draws (x, y, z), times
-          // radius, minus 0.5 per component.
-          double r0 = rand_double(st);
-          double r1 = rand_double(st);
-          double r2 = rand_double(st);
-          V3 off = v3(r0, r1, r2) * light->radius;
-          off = v3(off.x - 0.5, off.y - 0.5, off.z - 0.5);
-          V3 L = normalize(lpos + off - q);
-          // Light::distanceAttenuation, Light.cu:56-68
-          double dist = norm(lpos - q);
-          double fall = light->constant_term + (light->linear_term + light->quadratic_term * dist) * dist;
-          fall = (fabs(fall) < kRayEps) ? 1.0 : 1.0 / fall;
-          double datt = fmin(1.0, fall);
-          // Light::shadowAttenuation, Light.cu:5-37 (ray from q, no offset)
-          V3 satt = v3(1, 1, 1);
-          Hit sh_hit;
-          int sres = traverse(*s, q, L, true, &sh_hit);
-          if (sres < 0) overflow++;
-          sh = 0;
-          if (sres > 0 && sh_hit.t < norm(lpos - q)) {
-            const Material& om = s->mats[s->matid[sh_hit.id]];
-            if (sh_hit.t < kRayEps) {
-              satt = v3(1, 1, 1);
-            } else {
-              sh = 1;
-              shid = sh_hit.id;
-              // Trans() is isZero(kt) (inc/material.h:31), so an opaque
-              // occluder (kt = 0) passes kd % (1 - kt).
-              bool trans = om.kt[0] == 0 && om.kt[1] == 0 && om.kt[2] == 0;
-              if (trans)
-                satt = v3(om.kd[0] * (1 - om.kt[0]), om.kd[1] * (1 - om.kt[1]), om.kd[2] * (1 - om.kt[2]));
-              else
-                satt = v3(0, 0, 0);
-            }
-          }
-          V3 att = datt * satt;
-          double lam = dot(N, L);
-          if (lam < 0) lam = 0;
-          V3 diffuse = v3(m.kd[0] * lam, m.kd[1] * lam, m.kd[2] * lam);
-          V3 R = (-2.0 * dot(L, N)) * N + L;
-          R = normalize(R);
-          double sp = dot(R, Vv);
-          sp = (double)powf((float)fmax(0.0, sp), (float)m.shininess);
-          V3 spec = v3(m.ks[0] * sp, m.ks[1] * sp, m.ks[2] * sp);
-          I = I + mulc(mulc(att, diffuse + spec), lcol);
-          col = I;
-        } else {
+        if (res > 0)
+          col = shade_hit(*s, cam, light, org, dir, hh, hit_normal(*s, hh), st, &sh, &shid, &overflow);
+        else
           col = v3(0.9, 0.9, 0.9);
-        }
         acc = acc + col;
         if (hit_id) hit_id[si] = res > 0 ? hh.id : -1;
         if (hit_t) hit_t[si] = res > 0 ? hh.t : 0.0;
@@ -657,6 +722,79 @@ int orc_render(void* h, const orc_camera* cam, const orc_light* light, int W, in
       }
       // AverageSuperSamplingKernel clamp (scene.cu:127-140), then
       // pullRaytracedImage's (unsigned char)(255.0*x) (inc/raytracer.h:53-63).
+      double cc[3] = {acc.x, acc.y, acc.z};
+      for (int ch = 0; ch < 3; ch++) {
+        double v = cc[ch];
+        if (v < 0) v = 0.0;
+        if (v > 1) v = 1.0;
+        if (rgb8) rgb8[3 * (size_t)idx + ch] = (uint8_t)(255.0 * v);
+      }
+    }
+  }
+  return overflow;
+}
+
+// orc_render with recursive traceRay (trace_rec): up to `depth` levels of
+// reflected and refracted rays below each primary ray, whose shading draws
+// from the pixel's stream in depth-first order.  optics[4*m] = kr xyz, ior of
+// material m; NULL takes kr = ks (Scene_h::LoadObj sets kr to the MTL's
+// specular colour, src/scene.cpp:29) and ior = 1 (tinyobjloader's default).
+// Outputs as orc_render (hit_id/hit_t: the primary ray's closest hit).
+int orc_render_rec(void* h, const orc_camera* cam, const orc_light* light, int W, int H, int spp, int depth,
+                   const double* optics, uint8_t* rgb8, double* color, int* hit_id, double* hit_t,
+                   const double* rays_in, double* rays_out, int nthreads) {
+  const Scene* s = (const Scene*)h;
+  std::vector<double> opt(4 * (size_t)s->nmat);
+  for (int m = 0; m < s->nmat; m++) {
+    for (int c = 0; c < 3; c++) opt[4 * m + c] = optics ? optics[4 * m + c] : s->mats[m].ks[c];
+    opt[4 * m + 3] = optics ? optics[4 * m + 3] : 1.0;
+  }
+  const int gx = (W + 15) / 16;
+  int overflow = 0;
+  const double invW = 1.0 / double(W), invH = 1.0 / double(H);
+  const double aspect = double(W) / double(H);
+  const double angle = tan(M_PI * 0.5 * cam->fov / 180.0f);
+  const double aperture = 1 / cam->fstop;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for collapse(2) schedule(dynamic, 16) reduction(+ : overflow)
+#endif
+  for (int py = 0; py < H; py++) {
+    for (int px = 0; px < W; px++) {
+      const int idx = (H - py - 1) * W + px;
+      uint32_t st = wang_hash((uint32_t)(((py / 16) * gx + px / 16) * 256 + (py % 16) * 16 + (px % 16)));
+      double xx = (2 * ((px + 0.5) * invW) - 1) * angle * aspect;
+      double yy = (1 - 2 * ((py + 0.5) * invH)) * angle;
+      V3 acc = v3(0, 0, 0);
+      for (int k = 0; k < spp; k++) {
+        const size_t si = (size_t)idx * spp + k;
+        double dofAngle = 2 * M_PI * rand_double(st);
+        double dofRadius = aperture * sqrt(rand_double(st)) / 2.0;
+        V3 org = v3(dofRadius * cos(dofAngle), dofRadius * sin(dofAngle), 0);
+        V3 dir = v3(xx, yy, -1.0);
+        dir = normalize(dir) * cam->focal_point - org;
+        dir = normalize(dir);
+        if (rays_in) {
+          const double* r = rays_in + 6 * si;
+          org = v3(r[0], r[1], r[2]);
+          dir = v3(r[3], r[4], r[5]);
+        }
+        if (rays_out) {
+          double* r = rays_out + 6 * si;
+          r[0] = org.x, r[1] = org.y, r[2] = org.z, r[3] = dir.x, r[4] = dir.y, r[5] = dir.z;
+        }
+        Hit first;
+        int res = 0;
+        int ov = 0;
+        acc = acc + trace_rec(*s, cam, light, opt.data(), org, dir, depth, st, &ov, &first, &res);
+        overflow += ov;
+        if (hit_id) hit_id[si] = res > 0 ? first.id : -1;
+        if (hit_t) hit_t[si] = res > 0 ? first.t : 0.0;
+      }
+      acc = v3(acc.x / double(spp), acc.y / double(spp), acc.z / double(spp));
+      if (color) {
+        color[3 * (size_t)idx] = acc.x, color[3 * (size_t)idx + 1] = acc.y, color[3 * (size_t)idx + 2] = acc.z;
+      }
       double cc[3] = {acc.x, acc.y, acc.z};
       for (int ch = 0; ch < 3; ch++) {
         double v = cc[ch];

@@ -161,6 +161,38 @@ class OracleScene:
         return out
 
 
+def _render_rec(self, cam, light, width, height, spp, depth, optics=None, rays_in=None, rays_out=False, nthreads=0):
+    """orc_render_rec: traceRay with `depth` levels of reflection and
+    refraction.  optics: (num_materials, 4) kr xyz + ior, or None (kr = ks,
+    ior = 1)."""
+    assert self.kind == "oracle"
+    c = _Cam(cam.fov, cam.focal_point, cam.fstop, (C.c_double * 3)(*cam.eye))
+    L = _Light((C.c_double * 3)(*light.color), (C.c_double * 3)(*light.position), light.radius,
+               light.constant_term, light.linear_term, light.quadratic_term)
+    npx = width * height
+    rgb = np.zeros((npx, 3), np.uint8)
+    col = np.zeros((npx, 3), np.float64)
+    hid = np.zeros(npx * spp, np.int32)
+    ht = np.zeros(npx * spp, np.float64)
+    ro = np.zeros((npx * spp, 6), np.float64) if rays_out else None
+    ri = None if rays_in is None else np.ascontiguousarray(rays_in, np.float64)
+    op = None if optics is None else np.ascontiguousarray(optics, np.float64).reshape(-1, 4)
+    g = lambda a: None if a is None else a.ctypes.data  # noqa: E731
+    f = self.lib.orc_render_rec
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.POINTER(_Cam), C.POINTER(_Light), C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p,
+                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+    ov = f(self.h, C.byref(c), C.byref(L), width, height, spp, depth, g(op), rgb.ctypes.data, col.ctypes.data,
+           hid.ctypes.data, ht.ctypes.data, g(ri), g(ro), nthreads)
+    out = dict(rgb=rgb, color=col, hit_id=hid, hit_t=ht, overflow=ov)
+    if rays_out:
+        out["rays"] = ro
+    return out
+
+
+OracleScene.render_recursive = _render_rec
+
+
 def _adjoint(self, cam, light, width, height, spp, grad_rgb, grad_depth=None, nthreads=0):
     """Float64 reference gradient (orc_adjoint)."""
     assert self.kind == "oracle"

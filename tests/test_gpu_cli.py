@@ -93,3 +93,60 @@ def test_cli_errors(cli_scene, tmp_path):
     assert r.returncode != 0 and "bad value" in r.stderr
     r = subprocess.run([cli, "--bogus"], capture_output=True, text=True, timeout=60)
     assert r.returncode != 0
+
+
+def write_materials_scene(d, mesh, ior):
+    """An OBJ/MTL pair holding `mesh` with one MTL entry per material row
+    (Kd, Ks, Kt, Ke, Ns, and Ni from `ior`)."""
+    names = [f"m{k}" for k in range(len(mesh.materials))]
+    with open(os.path.join(d, "optics.mtl"), "w") as f:
+        for name, m, n in zip(names, mesh.materials, ior):
+            f.write(f"newmtl {name}\n")
+            for key, at in (("Kd", 3), ("Ks", 6), ("Kt", 9), ("Ke", 12)):
+                f.write(key + " %.17g %.17g %.17g\n" % tuple(m[at:at + 3]))
+            f.write("Ns %.17g\nNi %.17g\n" % (m[15], n))
+    with open(os.path.join(d, "optics.obj"), "w") as f:
+        f.write("mtllib optics.mtl\n")
+        for v in mesh.verts:
+            f.write("v %.9g %.9g %.9g\n" % tuple(float(x) for x in v))
+        for n in mesh.normals:
+            f.write("vn %.9g %.9g %.9g\n" % tuple(float(x) for x in n))
+        cur = None
+        for a, b, m in zip(mesh.vidx + 1, mesh.nidx + 1, mesh.matid):
+            if m != cur:
+                f.write(f"usemtl {names[m]}\n")
+                cur = m
+            f.write("f %d//%d %d//%d %d//%d\n" % (a[0], b[0], a[1], b[1], a[2], b[2]))
+    return os.path.join(d, "optics.obj")
+
+
+def test_cli_depth_reflections_and_refractions(cli_scene, tmp_path):
+    """--depth 3 on a mirror, glass and diffuse scene: the CLI takes kr = Ks
+    and ior = Ni from the MTL (crt_obj_optics) and renders with
+    crt_render_recursive; compared with the oracle's recursive render of the
+    same OBJ.  Every material with Ks reflects and has a Phong highlight,
+    whose powf may round differently on the host: 8-bit values within 1."""
+    from crt import data
+    from oracle.oracle import OracleScene
+    from test_recursive import optics_scene
+    cli = cli_scene[0]
+    mesh, optics = optics_scene(specular=True)
+    obj = write_materials_scene(str(tmp_path), mesh, optics[:, 3])
+    bmp = str(tmp_path / "depth.bmp")
+    W, H, spp = 48, 32, 2
+    run_cli(cli, ["-i", obj, "-o", bmp, "-w", str(W), "-h", str(H), "-f", "inf", "-v", "50", "-P", "3",
+                  "-p", "2.5,3,-1.5", "-a", "1,0.02,0.01", "-R", "0", "--spp", str(spp), "--depth", "3"])
+    got = read_bmp(bmp)
+    back = data.load_obj(obj)
+    cam = data.Camera(fov=50.0, focal_point=3.0, fstop=math.inf)
+    light = data.Light(position=f32(2.5, 3, -1.5), radius=0.0, constant_term=1.0, linear_term=f32(0.02)[0],
+                       quadratic_term=f32(0.01)[0])
+    cli_optics = np.concatenate([back.materials[:, 6:9], optics[:, 3:4]], 1)
+    ref = OracleScene(back).render_recursive(cam, light, W, H, spp, 3, cli_optics)["rgb"]
+    plain = OracleScene(back).render(cam, light, W, H, spp=spp)["rgb"]
+    diff = np.abs(got.astype(int) - ref.astype(int))
+    assert diff.max() <= 1 and (diff == 0).mean() > 0.99
+    assert (got != plain).any(1).mean() > 0.05  # the reflections and refractions show
+    r = subprocess.run([cli, "-i", obj, "--depth", "9"], capture_output=True, text=True, timeout=60)
+    assert r.returncode != 0 and "bad value" in r.stderr
+

@@ -40,6 +40,7 @@ newmtl glass
 Kd 0.2 0.3 0.4
 Tf 0.9 0.9 0.9
 Ke 0.01 0.02 0.03
+Ni 1.45
 """
 
 
@@ -63,6 +64,16 @@ def test_native_reader_matches_python_reader(scene_dir):
     assert list(a.matid) == [0, 0, 0, 1, 1, 1, 1]  # unknown material -> 0
     assert a.materials[0, 15] == 32.0 and a.materials[1, 15] == 1.0  # tinyobjloader's default Ns
     assert np.array_equal(a.materials[1, 9:12], [0.9, 0.9, 0.9])  # Tf is the transmittance
+
+
+def test_obj_optics_take_ks_and_ni(scene_dir):
+    """crt_obj_optics: kr = Ks (Scene_h::LoadObj's `mat.kr = specular`,
+    src/scene.cpp:29) and ior = Ni, tinyobjloader's 1 where Ni is absent."""
+    import crt
+    mesh, optics = crt.load_obj_native(str(scene_dir / "scene.obj"), with_optics=True)
+    assert optics.shape == (2, 4)
+    assert np.array_equal(optics[:, :3], mesh.materials[:, 6:9])
+    assert np.array_equal(optics[:, 3], [1.0, 1.45])
 
 
 def test_native_reader_rejects_faces_without_normals(tmp_path, built):
