@@ -96,6 +96,7 @@ def lib():
             "crt_trace_shadow": [vp, vp, i64, vp, vp, vp],
             "crt_render": [vp, vp, vp, vp, vp, vp],
             "crt_render_recursive": [vp, vp, vp, vp, i32, vp, vp, vp],
+            "crt_set_lens_tables": [i32],
             "crt_morton": [vp, vp, i32, vp, vp, vp],
             "crt_sort_pairs": [vp, vp, vp, vp, i32, i32, vp],
             "crt_sort_pairs_noalloc": [vp, vp, vp, vp, i32, i32, vp],

@@ -230,6 +230,9 @@ crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* v
   v.wnodes = bb.wnodes, v.leaves = bb.leaves, v.g = bb.g, v.args = b->args;
   v.counter = bb.counters + 4;
   // per-mesh render arguments
+  bool lens = false;
+  for (int m = 0; m < M; m++) lens = lens || 1 / views[m].camera.fstop != 0.0;
+  const LensTables lt = lens ? lens_tables(st) : LensTables{};
   std::vector<RenderArgs> ha(M);
   for (int m = 0; m < M; m++) {
     const crt_batch_view& w = views[m];
@@ -250,6 +253,7 @@ crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* v
     a.lradius = w.light.radius;
     a.latt[0] = w.light.constant_term, a.latt[1] = w.light.linear_term, a.latt[2] = w.light.quadratic_term;
     a.rgb8 = b->image + 3 * (size_t)b->px_off[m];
+    a.lens_cs = lt.cs, a.lens_sqrt = lt.sq;
   }
   static_assert(sizeof(DMat) == sizeof(crt_material), "material layout");
   auto up = [&](void* dst, const void* src, size_t n) {

@@ -391,7 +391,7 @@ crt_status crt_trace_shadow(crt_scene* s, const double* rays, int64_t n, int32_t
 // and crt_adjoint_lambert (the constants of raytracer.cu:126-130, 144; tan on
 // the host).  Outputs start unset.
 static crt_status render_args(crt_scene* s, const crt_camera* cam, const crt_light* light,
-                              const crt_render_params* p, RenderArgs& a) {
+                              const crt_render_params* p, cudaStream_t st, RenderArgs& a) {
   if (!s->built) return fail(CRT_NOT_BUILT, "no BVH");
   if (p->width <= 0 || p->height <= 0 || p->spp <= 0) return fail(CRT_INVALID_ARG, "width, height, spp must be > 0");
   if ((int64_t)p->width * p->height > (int64_t)1 << 30) return fail(CRT_INVALID_ARG, "image too large");
@@ -415,6 +415,10 @@ static crt_status render_args(crt_scene* s, const crt_camera* cam, const crt_lig
   a.lradius = light->radius;
   a.latt[0] = light->constant_term, a.latt[1] = light->linear_term, a.latt[2] = light->quadratic_term;
   a.counter = s->counter;
+  if (a.aperture != 0.0) {
+    const LensTables t = lens_tables(st);
+    a.lens_cs = t.cs, a.lens_sqrt = t.sq;
+  }
   return CRT_OK;
 }
 
@@ -422,8 +426,8 @@ crt_status crt_render(crt_scene* s, const crt_camera* cam, const crt_light* ligh
                       const crt_render_out* o, void* stream) {
   if (!s || !cam || !light || !p || !o) return fail(CRT_INVALID_ARG, "null argument");
   RenderArgs a;
-  if (crt_status e = render_args(s, cam, light, p, a)) return e;
   cudaStream_t st = S(stream);
+  if (crt_status e = render_args(s, cam, light, p, st, a)) return e;
   const size_t npx = (size_t)p->width * p->height;
   const size_t nsm = npx * (size_t)p->spp;
   // outputs: whole-image buffers; a row band writes only its rows
@@ -475,8 +479,8 @@ crt_status crt_render_recursive(crt_scene* s, const crt_camera* cam, const crt_l
   if (o->traversal_stats || o->shadow || o->shadow_id || o->depth)
     return fail(CRT_INVALID_ARG, "crt_render_recursive writes rgb8, rgb_f32, rgb_f64, hit_id, hit_t and rays only");
   RenderArgs a;
-  if (crt_status e = render_args(s, cam, light, p, a)) return e;
   cudaStream_t st = S(stream);
+  if (crt_status e = render_args(s, cam, light, p, st, a)) return e;
   // kr and ior per material (host or device array); NULL: the kernel takes
   // kr = ks and ior = 1
   static_assert(sizeof(DOptics) == sizeof(crt_optics) && kMaxRecDepth == CRT_MAX_DEPTH, "crt_optics layout");
@@ -524,8 +528,8 @@ crt_status crt_adjoint_lambert(crt_scene* s, const crt_camera* cam, const crt_li
                                double* grad_vertices, double* grad_light, double* grad_kd, void* stream) {
   if (!s || !cam || !light || !p || !grad_rgb) return fail(CRT_INVALID_ARG, "null argument");
   RenderArgs a;
-  if (crt_status e = render_args(s, cam, light, p, a)) return e;
   cudaStream_t st = S(stream);
+  if (crt_status e = render_args(s, cam, light, p, st, a)) return e;
   const size_t npx = (size_t)p->width * p->height;
   DevView vg, vgd;
   CRT_CUDA(vg.open(const_cast<double*>(grad_rgb), 3 * sizeof(double) * npx, true, st), "stage grad_rgb");

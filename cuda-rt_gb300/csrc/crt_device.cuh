@@ -554,6 +554,19 @@ __device__ __forceinline__ void scene_consts(const DScene& S, float rb[6], float
   D = __fmul_ru(1.7320509f, ord2f(S.g->emax));
 }
 
+// True when shade()'s Phong term cannot change the colour (material.cu:30-
+// 36), so it need not be evaluated: ks = 0 and 0 <= shininess <= 1e6 make
+// the term ks * powf(max(0, R.V), shininess) a signed zero (R and V are unit
+// vectors, so the base is at most 1 + 2^-21 and the power is finite), and
+// d + (+-0) is d unless d is itself a zero; a zero d gives a zero product
+// att * d * lcol (or NaN whatever the sign), and I + (+-0) is I unless I is
+// -0.  So the colour is the same bit for bit unless some I component is -0.
+__device__ __forceinline__ bool phong_vanishes(const DMat& m, const D3& I) {
+  const long long neg0 = (long long)0x8000000000000000ull;
+  return m.ks[0] == 0.0 && m.ks[1] == 0.0 && m.ks[2] == 0.0 && m.shininess >= 0.0 && m.shininess <= 1e6 &&
+         __double_as_longlong(I.x) != neg0 && __double_as_longlong(I.y) != neg0 && __double_as_longlong(I.z) != neg0;
+}
+
 // Smooth normal of a hit, bvh.cu:357-364.
 __device__ __forceinline__ D3 hit_normal(const DScene& S, const HitRec& h) {
   const int na = S.nidx[3 * h.id], nb = S.nidx[3 * h.id + 1], nc = S.nidx[3 * h.id + 2];
@@ -581,9 +594,51 @@ __device__ __forceinline__ uint32_t wang_hash(uint32_t seed) {
   return seed;
 }
 // randDouble: the 32-bit draw is rounded to float, then scaled by 2^-32.
+__device__ __forceinline__ double draw_value(float f) { return (double)f * 2.3283064365386963e-10; }
 __device__ __forceinline__ double rand_double(uint32_t& s) {
   const uint32_t v = xorshift32(s);
-  return (double)__uint2float_rn(v) * 2.3283064365386963e-10;
+  return draw_value(__uint2float_rn(v));
+}
+
+// ---------------------------------------------------------------- lens
+// A draw is (double)(float)v * 2^-32, so it takes one of kLensValues values:
+// the floats that are integers in [0, 2^32], 2^24 below 2^24 and 2^23 in each
+// of the eight binades above.  lens_index numbers them densely.
+constexpr uint32_t kLensValues = 83886081u;
+__device__ __forceinline__ uint32_t lens_index(float f) {
+  return f < 16777216.f ? (uint32_t)f : 16777216u + (__float_as_uint(f) - 0x4B800000u);
+}
+__device__ __forceinline__ float lens_value(uint32_t i) {
+  return i < 16777216u ? (float)i : __uint_as_float(0x4B800000u + (i - 16777216u));
+}
+// cos and sin of the lens angle 2*pi*u and sqrt(u) of the lens radius draw
+// u, as runRayTracerKernelRec computes them (raytracer.cu:141-142).
+__device__ __forceinline__ void lens_angle(double u, double& ca, double& sa) {
+  sincos(2 * 3.14159265358979323846 * u, &sa, &ca);
+}
+
+// The thin-lens origin of one sample (raytracer.cu:141-144): two draws, the
+// angle's and the radius's, and (dofRadius cos, dofRadius sin, 0).  With
+// tables (cs[i] = cos/sin and sq[i] = sqrt at draw value i, built from the
+// same expressions) the double sincos and sqrt become two loads; the result
+// is the same either way.  A zero radius gives +-0 components, which no later
+// operation can tell apart from 0.
+__device__ __forceinline__ void lens_origin(const double2* cs, const double* sq, double aperture, uint32_t& st,
+                                            double& ox, double& oy) {
+  const float f1 = __uint2float_rn(xorshift32(st)), f2 = __uint2float_rn(xorshift32(st));
+  const double root = sq ? __ldg(sq + lens_index(f2)) : sqrt(draw_value(f2));
+  const double dofRadius = aperture * root / 2.0;
+  ox = 0.0, oy = 0.0;
+  if (dofRadius != 0.0) {
+    double ca, sa;
+    if (cs) {
+      const double2 c = __ldg(cs + lens_index(f1));
+      ca = c.x, sa = c.y;
+    } else {
+      lens_angle(draw_value(f1), ca, sa);
+    }
+    ox = dofRadius * ca, oy = dofRadius * sa;
+  }
 }
 
 }  // namespace crt

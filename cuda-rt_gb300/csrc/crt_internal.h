@@ -107,6 +107,8 @@ struct RenderArgs {
   double* rgbd = nullptr;     // optional: mean colour in double
   double* depth = nullptr;    // optional: mean hit t (misses count 0)
   int* shadow_id = nullptr;   // optional: occluding triangle per sample, -1 if none
+  const double2* lens_cs = nullptr;  // optional lens tables (lens.cu)
+  const double* lens_sqrt = nullptr;
   // adjoint (grad_rgb != NULL selects it)
   const double* grad_rgb = nullptr;
   const double* grad_depth = nullptr;
@@ -115,6 +117,15 @@ struct RenderArgs {
   double* grad_albedo = nullptr;
 };
 cudaError_t launch_render(const DScene& S, const RenderArgs& a, cudaStream_t st);
+
+// lens.cu: the thin-lens tables of the current device (built on first use
+// when enabled and memory allows; otherwise both NULL, and the kernels
+// compute the same values inline).
+struct LensTables {
+  const double2* cs = nullptr;
+  const double* sq = nullptr;
+};
+LensTables lens_tables(cudaStream_t st);
 
 // recursive.cu: traceRay with reflected and refracted rays, at most
 // kMaxRecDepth levels below the primary ray.  optics[m] (device, may be

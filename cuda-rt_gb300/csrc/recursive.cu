@@ -102,14 +102,9 @@ struct PixelRay {
 // Primary ray of the next sample: two draws (lens angle and radius), the
 // thin-lens ray of runRayTracerKernelRec (raytracer.cu:141-152).
 __device__ __forceinline__ PixelRay primary(const RenderArgs& A, D3 fdir, uint32_t& st) {
-  const double dofAngle = 2 * 3.14159265358979323846 * rand_double(st);
-  const double dofRadius = A.aperture * sqrt(rand_double(st)) / 2.0;
-  D3 org = d3(0.0, 0.0, 0.0);
-  if (dofRadius != 0.0) {
-    double sa, ca;
-    sincos(dofAngle, &sa, &ca);
-    org = d3(dofRadius * ca, dofRadius * sa, 0.0);
-  }
+  double ox, oy;
+  lens_origin(A.lens_cs, A.lens_sqrt, A.aperture, st, ox, oy);
+  const D3 org = d3(ox, oy, 0.0);
   return PixelRay{org, normalize_exact(fdir - org)};
 }
 

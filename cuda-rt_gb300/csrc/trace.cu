@@ -135,16 +135,11 @@ __device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int 
               xorshift32(st);
             }
           }
-          const double dofAngle = 2 * 3.14159265358979323846 * rand_double(st);
-          const double dofRadius = A.aperture * sqrt(rand_double(st)) / 2.0;
-          org = d3(0.0, 0.0, 0.0);
-          if (dofRadius != 0.0) {  // a zero radius gives +-0 components, which no later operation can tell apart
-            // sincos gives sin and cos bit for bit (checked for every angle 2*pi*u
-            // the float-valued mrand draw u can take)
-            double sa, ca;
-            sincos(dofAngle, &sa, &ca);
-            org = d3(dofRadius * ca, dofRadius * sa, 0.0);
-          }
+          // sincos gives sin and cos bit for bit (checked for every angle 2*pi*u
+          // the float-valued mrand draw u can take)
+          double ox, oy;
+          lens_origin(A.lens_cs, A.lens_sqrt, A.aperture, st, ox, oy);
+          org = d3(ox, oy, 0.0);
           dir = normalize_exact(fdir - org);
           ray_setup(rc, org.x, org.y, org.z, dir.x, dir.y, dir.z, B, D);
         } else {
@@ -190,7 +185,7 @@ __device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int 
       HitRec s;
       const int sres = traverse<true, MODE == kRenderStats, SHORT>(S, sr, rb, s, hit, &ts, ring);
       if (sres < 0) atomicOr(&S.g->err, kErrStack);
-      D3 N, V;
+      D3 N;
       double sN = 0.0, fall = 0.0, datt = 0.0;
       bool tiny = false;
       if (hit) {
@@ -202,8 +197,6 @@ __device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int 
         const D3 Nr = (1.0 - (h.alpha + h.beta)) * nA + h.alpha * nB + h.beta * nC;
         sN = 1.0 / (double)sqrtf(__double2float_rn(Nr.x * Nr.x + Nr.y * Nr.y + Nr.z * Nr.z));
         N = d3(Nr.x * sN, Nr.y * sN, Nr.z * sN);
-        V = d3(A.eye[0], A.eye[1], A.eye[2]) - q;
-        V = normalize_exact(d3(-V.x, -V.y, -V.z));
         // Light::distanceAttenuation
         fall = A.latt[0] + (A.latt[1] + A.latt[2] * dist) * dist;
         tiny = fabs(fall) < kRayEps;
@@ -235,12 +228,17 @@ __device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int 
         double lam = NL;
         if (lam < 0) lam = 0;
         const D3 diffuse = d3(m.kd[0] * lam, m.kd[1] * lam, m.kd[2] * lam);
-        D3 R = (-2.0 * dot(L, N)) * N + L;
-        R = normalize_exact(R);
-        double sp = dot(R, V);
-        sp = (double)powf(__double2float_rn(fmax(0.0, sp)), __double2float_rn(m.shininess));
-        const D3 spec = d3(m.ks[0] * sp, m.ks[1] * sp, m.ks[2] * sp);
-        const D3 ds = diffuse + spec;
+        D3 ds = diffuse;
+        if (!phong_vanishes(m, I)) {
+          D3 V = d3(A.eye[0], A.eye[1], A.eye[2]) - q;
+          V = normalize_exact(d3(-V.x, -V.y, -V.z));
+          D3 R = (-2.0 * dot(L, N)) * N + L;
+          R = normalize_exact(R);
+          double sp = dot(R, V);
+          sp = (double)powf(__double2float_rn(fmax(0.0, sp)), __double2float_rn(m.shininess));
+          const D3 spec = d3(m.ks[0] * sp, m.ks[1] * sp, m.ks[2] * sp);
+          ds = diffuse + spec;
+        }
         I = I + d3(att.x * ds.x * A.lcol[0], att.y * ds.y * A.lcol[1], att.z * ds.z * A.lcol[2]);
         col = I;
         if (MODE == kAdjoint) {

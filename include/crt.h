@@ -181,6 +181,17 @@ crt_status crt_render_recursive(crt_scene* scene, const crt_camera* camera, cons
                                 const crt_render_params* params, int32_t depth, const crt_optics* optics,
                                 const crt_render_out* out, void* stream);
 
+/* Thin-lens sample tables (no counterpart in the reference).  Each
+ * thin-lens sample needs cos/sin(2*pi*u1) and sqrt(u2) in double for two
+ * mrand draws (raytracer.cu:141-142); a draw takes one of 83,886,081
+ * values, so the library tabulates both functions at every value once per
+ * device (2.0 GB of device memory, built in about 10 ms by the same double
+ * expressions) and the kernels load them instead of computing them.  Images
+ * are identical either way.  On by default; built at the first thin-lens
+ * render or batch creation on a device with 8 GB to spare, outside stream
+ * capture.  enable = 0 turns them off for later calls (the memory stays). */
+crt_status crt_set_lens_tables(int32_t enable);
+
 /* Replace the material table (same count as at creation), e.g. new
  * per-triangle albedos.  Asynchronous. */
 crt_status crt_scene_set_materials(crt_scene* scene, const crt_material* materials, int32_t num_materials,
