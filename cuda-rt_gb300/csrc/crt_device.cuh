@@ -567,6 +567,20 @@ __device__ __forceinline__ bool phong_vanishes(const DMat& m, const D3& I) {
          __double_as_longlong(I.x) != neg0 && __double_as_longlong(I.y) != neg0 && __double_as_longlong(I.z) != neg0;
 }
 
+// Material::shade's Phong term ks * powf(max(0, R.V), shininess)
+// (material.cu:17-20, 30-35) at q with unit light direction L and normal N;
+// V is the direction from the eye to q.  Out of line: Lambert materials skip
+// it (phong_vanishes), and its powf would sit in the hot loop's code.
+static __device__ __noinline__ D3 phong_term(const DMat* __restrict__ m, D3 L, D3 N, D3 q, D3 eye) {
+  D3 V = eye - q;
+  V = normalize_exact(d3(-V.x, -V.y, -V.z));
+  D3 R = (-2.0 * dot(L, N)) * N + L;
+  R = normalize_exact(R);
+  double sp = dot(R, V);
+  sp = (double)powf(__double2float_rn(fmax(0.0, sp)), __double2float_rn(m->shininess));
+  return d3(m->ks[0] * sp, m->ks[1] * sp, m->ks[2] * sp);
+}
+
 // Smooth normal of a hit, bvh.cu:357-364.
 __device__ __forceinline__ D3 hit_normal(const DScene& S, const HitRec& h) {
   const int na = S.nidx[3 * h.id], nb = S.nidx[3 * h.id + 1], nc = S.nidx[3 * h.id + 2];
@@ -612,10 +626,13 @@ __device__ __forceinline__ float lens_value(uint32_t i) {
   return i < 16777216u ? (float)i : __uint_as_float(0x4B800000u + (i - 16777216u));
 }
 // cos and sin of the lens angle 2*pi*u and sqrt(u) of the lens radius draw
-// u, as runRayTracerKernelRec computes them (raytracer.cu:141-142).
-__device__ __forceinline__ void lens_angle(double u, double& ca, double& sa) {
+// u, as runRayTracerKernelRec computes them (raytracer.cu:141-142).  Out of
+// line: with the lens tables the pixel kernels never call them, and code
+// inside the hot loop costs instruction-cache misses even when skipped.
+static __device__ __noinline__ void lens_angle(double u, double& ca, double& sa) {
   sincos(2 * 3.14159265358979323846 * u, &sa, &ca);
 }
+static __device__ __noinline__ double lens_root(double u) { return sqrt(u); }
 
 // The thin-lens origin of one sample (raytracer.cu:141-144): two draws, the
 // angle's and the radius's, and (dofRadius cos, dofRadius sin, 0).  With
@@ -626,7 +643,7 @@ __device__ __forceinline__ void lens_angle(double u, double& ca, double& sa) {
 __device__ __forceinline__ void lens_origin(const double2* cs, const double* sq, double aperture, uint32_t& st,
                                             double& ox, double& oy) {
   const float f1 = __uint2float_rn(xorshift32(st)), f2 = __uint2float_rn(xorshift32(st));
-  const double root = sq ? __ldg(sq + lens_index(f2)) : sqrt(draw_value(f2));
+  const double root = sq ? __ldg(sq + lens_index(f2)) : lens_root(draw_value(f2));
   const double dofRadius = aperture * root / 2.0;
   ox = 0.0, oy = 0.0;
   if (dofRadius != 0.0) {

@@ -184,8 +184,6 @@ __global__ void __launch_bounds__(128) k_pixels_rec(DScene S, RenderArgs A, cons
         mid = __ldg(S.matid + h.id);
         const DMat& m = S.mats[mid];
         D3 I = d3(m.ke[0] + m.ka[0] * 0.0, m.ke[1] + m.ka[1] * 0.0, m.ke[2] + m.ka[2] * 0.0);
-        D3 V = d3(A.eye[0], A.eye[1], A.eye[2]) - q;
-        V = normalize_exact(d3(-V.x, -V.y, -V.z));
         double fall = A.latt[0] + (A.latt[1] + A.latt[2] * dist) * dist;
         fall = fabs(fall) < kRayEps ? 1.0 : 1.0 / fall;
         const double datt = fmin(1.0, fall);
@@ -200,10 +198,8 @@ __global__ void __launch_bounds__(128) k_pixels_rec(DScene S, RenderArgs A, cons
         double lam = dot(N, L);
         if (lam < 0) lam = 0;
         const D3 diffuse = d3(m.kd[0] * lam, m.kd[1] * lam, m.kd[2] * lam);
-        const D3 R = normalize_exact((-2.0 * dot(L, N)) * N + L);
-        double sp = dot(R, V);
-        sp = (double)powf(__double2float_rn(fmax(0.0, sp)), __double2float_rn(m.shininess));
-        const D3 ds = diffuse + d3(m.ks[0] * sp, m.ks[1] * sp, m.ks[2] * sp);
+        D3 ds = diffuse;
+        if (!phong_vanishes(m, I)) ds = diffuse + phong_term(S.mats + mid, L, N, q, d3(A.eye[0], A.eye[1], A.eye[2]));
         v = I + d3(att.x * ds.x * A.lcol[0], att.y * ds.y * A.lcol[1], att.z * ds.z * A.lcol[2]);
       }
       // depth-first walk: descend into this ray's first child, or return its

@@ -229,16 +229,7 @@ __device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int 
         if (lam < 0) lam = 0;
         const D3 diffuse = d3(m.kd[0] * lam, m.kd[1] * lam, m.kd[2] * lam);
         D3 ds = diffuse;
-        if (!phong_vanishes(m, I)) {
-          D3 V = d3(A.eye[0], A.eye[1], A.eye[2]) - q;
-          V = normalize_exact(d3(-V.x, -V.y, -V.z));
-          D3 R = (-2.0 * dot(L, N)) * N + L;
-          R = normalize_exact(R);
-          double sp = dot(R, V);
-          sp = (double)powf(__double2float_rn(fmax(0.0, sp)), __double2float_rn(m.shininess));
-          const D3 spec = d3(m.ks[0] * sp, m.ks[1] * sp, m.ks[2] * sp);
-          ds = diffuse + spec;
-        }
+        if (!phong_vanishes(m, I)) ds = diffuse + phong_term(S.mats + mid, L, N, q, d3(A.eye[0], A.eye[1], A.eye[2]));
         I = I + d3(att.x * ds.x * A.lcol[0], att.y * ds.y * A.lcol[1], att.z * ds.z * A.lcol[2]);
         col = I;
         if (MODE == kAdjoint) {
