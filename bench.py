@@ -58,10 +58,13 @@ def peaks():
 
 
 class Clocks:
-    """Samples nvidia-smi during the timed region."""
+    """Samples nvidia-smi (every 50 ms) during the timed region: the sampler
+    is started, and its first sample awaited, before the region begins; the
+    summary keeps the samples read between the region's start and its end."""
 
     def __init__(self, index=0):
         self.samples, self.proc, self.index = [], None, index
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
@@ -69,22 +72,28 @@ class Clocks:
              "clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            deadline = time.time() + 5.0
+            while not self.samples and time.time() < deadline and self.proc.poll() is None:
+                time.sleep(0.01)
         except OSError:
             self.proc = None
+        self.t0 = time.time()
         return self
 
     def _read(self):
         for line in self.proc.stdout:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) >= 7:
-                self.samples.append(parts)
+                self.samples.append([time.time()] + parts)
 
     def __exit__(self, *a):
+        self.t1 = time.time()
         if self.proc:
+            time.sleep(0.06)  # the sample that covers the region's last moments
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=2)
@@ -92,14 +101,16 @@ class Clocks:
                 self.proc.kill()
 
     def summary(self):
-        if not self.samples:
+        inside = [s[1:] for s in self.samples if self.t0 is not None and self.t0 <= s[0] <= self.t1 + 0.06]
+        samples = inside or [s[1:] for s in self.samples[-2:]]
+        if not samples:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        sm = [float(s[0]) for s in samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in samples if s[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].strip() == "Active"})
+        reasons = sorted({names[i] for s in samples for i in range(4) if s[3 + i].strip() == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(samples)}
 
 
 def dist_setup():

@@ -634,6 +634,28 @@ static __device__ __noinline__ void lens_angle(double u, double& ca, double& sa)
 }
 static __device__ __noinline__ double lens_root(double u) { return sqrt(u); }
 
+// Table loads that neither allocate in L1 nor keep their lines in L2 ahead
+// of other data (an evict-first L2 policy): the lens tables are read at
+// random, once per sample, and would otherwise push BVH nodes and the
+// threads' local memory out of L2.
+__device__ __forceinline__ uint64_t evict_first_policy() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ double2 ld_stream(const double2* p) {
+  double2 v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;"
+               : "=d"(v.x), "=d"(v.y)
+               : "l"(p), "l"(evict_first_policy()));
+  return v;
+}
+__device__ __forceinline__ double ld_stream(const double* p) {
+  double v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(evict_first_policy()));
+  return v;
+}
+
 // The thin-lens origin of one sample (raytracer.cu:141-144): two draws, the
 // angle's and the radius's, and (dofRadius cos, dofRadius sin, 0).  With
 // tables (cs[i] = cos/sin and sq[i] = sqrt at draw value i, built from the
@@ -643,13 +665,13 @@ static __device__ __noinline__ double lens_root(double u) { return sqrt(u); }
 __device__ __forceinline__ void lens_origin(const double2* cs, const double* sq, double aperture, uint32_t& st,
                                             double& ox, double& oy) {
   const float f1 = __uint2float_rn(xorshift32(st)), f2 = __uint2float_rn(xorshift32(st));
-  const double root = sq ? __ldg(sq + lens_index(f2)) : lens_root(draw_value(f2));
+  const double root = sq ? ld_stream(sq + lens_index(f2)) : lens_root(draw_value(f2));
   const double dofRadius = aperture * root / 2.0;
   ox = 0.0, oy = 0.0;
   if (dofRadius != 0.0) {
     double ca, sa;
     if (cs) {
-      const double2 c = __ldg(cs + lens_index(f1));
+      const double2 c = ld_stream(cs + lens_index(f1));
       ca = c.x, sa = c.y;
     } else {
       lens_angle(draw_value(f1), ca, sa);
