@@ -44,9 +44,10 @@ W, H, SPP = 1920, 1080, 16
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one k_pixels
 # launch of this frame, from an ncu --set full capture of this command; the
 # fetched bytes (the `achieved` numerator) are mostly served by L1 and L2.
-# Most of these bytes are the threads' local memory (traversal stacks and
-# register spills of 155,648 resident threads), written back from L2.
-RENDER_DRAM_BYTES = 1_870_012_672
+# Most of these bytes are the lens-table lookups (two random loads per
+# sample, each filling whole L2 lines) and the threads' local memory
+# (traversal stacks and register spills of 155,648 resident threads).
+RENDER_DRAM_BYTES = 10_596_541_696
 
 
 def peaks():
