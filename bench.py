@@ -226,6 +226,7 @@ def run_crt(args, dist, rank, ws):
     refit = run_refit_vs_rebuild() if (rank == 0 and not args.no_extras) else None
     batched = run_batched() if (rank == 0 and not args.no_extras) else None
     adjoint = run_adjoint() if (rank == 0 and not args.no_extras) else None
+    nextrows = run_next_rows() if (rank == 0 and not args.no_extras) else None
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(sc, args.cpu_seconds)
@@ -259,6 +260,8 @@ def run_crt(args, dist, rank, ws):
         line["batched_vs_plain"] = batched
     if adjoint is not None:
         line["adjoint"] = adjoint
+    if nextrows is not None:
+        line["next_rows"] = nextrows
     if cpu is not None:
         line["cpu_baseline"] = cpu
     return line
@@ -421,6 +424,101 @@ def run_adjoint(reps=5):
             "loss": round(float(((img - t_img) ** 2).sum()), 6)}
 
 
+def run_next_rows(reps=3):
+    """The rows next to the path, each timed: (1) OBJ/MTL ingestion of the
+    200,000-face icosphere written as an OBJ (crt_obj_load, host); (2) full
+    shade -- Phong highlights and an area light (radius 0.3, three draws per
+    hit) against Lambert with a point light, 1280x720x4, on the mirror/glass
+    scene with an 81,920-face glass sphere; (3) reflections and refractions
+    to depth 3 on that scene (crt_render_recursive) against depth 0; (4) the
+    drop-in CLI end to end (process start, OBJ load, build, 1024x1024x20
+    thin-lens render, BMP write) on the OBJ of (1)."""
+    import shutil
+    import tempfile
+
+    import torch
+
+    import crt
+    from crt import build as cbuild
+    from crt import data
+    res = {}
+    tmp = tempfile.mkdtemp(prefix="crt_next_")
+    try:
+        # (1) ingestion
+        m = data.config4().mesh
+        obj = os.path.join(tmp, "ico.obj")
+        with open(os.path.join(tmp, "ico.mtl"), "w") as f:
+            f.write("newmtl lambert\nKd 0.8 0.8 0.8\n")
+        with open(obj, "w") as f:
+            f.write("mtllib ico.mtl\n")
+            np.savetxt(f, m.verts, fmt="v %.9g %.9g %.9g")
+            np.savetxt(f, m.normals, fmt="vn %.9g %.9g %.9g")
+            f.write("usemtl lambert\n")
+            np.savetxt(f, np.stack([m.vidx + 1, m.nidx + 1], 2).reshape(-1, 6), fmt="f %d//%d %d//%d %d//%d")
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            crt.load_obj_native(obj)
+            ts.append(time.perf_counter() - t0)
+        t = float(np.median(ts))
+        res["obj_ingest"] = {"triangles": m.ntri, "mbytes": round(os.path.getsize(obj) / 1e6, 1),
+                             "ms": round(t * 1e3, 1), "mtris_s": round(m.ntri / t / 1e6, 2)}
+        # (2), (3) shading and recursion
+        W2, H2, spp = 1280, 720, 4
+        stream = torch.cuda.current_stream()
+        rgb = torch.empty((W2 * H2, 3), dtype=torch.uint8, device="cuda")
+
+        def timed(fn):
+            fn()
+            torch.cuda.synchronize()
+            out = []
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                out.append(e0.elapsed_time(e1))
+            return float(np.median(out))
+
+        cam = data.Camera(fov=50.0, focal_point=3.0, fstop=1.0 / (2 * 0.02))
+        lt = data.light_for((2.0, 2.5, -2.0), (0.0, 0.0, -3.0))
+        point = data.Light(position=lt, linear_term=0.02, quadratic_term=0.01)
+        area = data.Light(position=lt, radius=0.3, linear_term=0.02, quadratic_term=0.01)
+        lam_mesh, optics = data.optics_scene(nu=64)
+        spec_mesh, _ = data.optics_scene(nu=64, specular=True)
+        g_lam, g_spec = crt.Scene(lam_mesh), crt.Scene(spec_mesh)
+        t_lam = timed(lambda: g_lam.render(cam, point, W2, H2, spp, out={"rgb8": rgb}, stream=stream))
+        t_full = timed(lambda: g_spec.render(cam, area, W2, H2, spp, out={"rgb8": rgb}, stream=stream))
+        rays = W2 * H2 * spp
+        res["full_shade"] = {"triangles": spec_mesh.ntri, "image": f"{W2}x{H2}x{spp}spp",
+                             "lambert_point_ms": round(t_lam, 3), "phong_area_ms": round(t_full, 3),
+                             "phong_area_mrays_s": round(rays / t_full / 1e3, 1)}
+        d_optics = torch.tensor(optics, dtype=torch.float64, device="cuda")
+        t_d0 = timed(lambda: g_spec.render_recursive(cam, area, W2, H2, spp, 0, d_optics, out={"rgb8": rgb},
+                                                     stream=stream))
+        t_d3 = timed(lambda: g_spec.render_recursive(cam, area, W2, H2, spp, 3, d_optics, out={"rgb8": rgb},
+                                                     stream=stream))
+        g_lam.check()
+        g_spec.check()
+        res["recursive"] = {"triangles": spec_mesh.ntri, "image": f"{W2}x{H2}x{spp}spp", "depth": 3,
+                            "depth0_ms": round(t_d0, 3), "depth3_ms": round(t_d3, 3),
+                            "primary_mrays_s": round(rays / t_d3 / 1e3, 1)}
+        # (4) the CLI
+        cli = cbuild.build_cli()
+        bmp = os.path.join(tmp, "out.bmp")
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            subprocess.run([cli, "-i", obj, "-o", bmp, "-w", "1024", "-h", "1024", "-R", "0"], check=True,
+                           capture_output=True, timeout=300)
+            ts.append(time.perf_counter() - t0)
+        res["cli"] = {"triangles": m.ntri, "image": "1024x1024x20spp thin lens", "seconds": round(float(np.median(ts)), 3)}
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return res
+
+
 def _cpu_impl():
     from oracle import oracle as orc
     kind = "port"
@@ -497,7 +595,7 @@ def main():
     ap.add_argument("--impl", default="crt", choices=["crt", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-extras", action="store_true", help="skip the refit-vs-rebuild, batched-vs-plain and adjoint figures")
+    ap.add_argument("--no-extras", action="store_true", help="skip the refit-vs-rebuild, batched-vs-plain, adjoint and next-row figures")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "crt" else args.warmup
     dist, rank, ws = dist_setup()

@@ -275,18 +275,24 @@ class Scene:
 
 
     def render_recursive(self, camera, light, width, height, spp, depth, optics=None, rows=None, rays=False,
-                         stream=None):
+                         out=None, stream=None):
         """crt_render_recursive: traceRay with `depth` levels of reflected and
         refracted rays.  optics: (num_materials, 4) array of kr xyz and ior,
         or None (kr = ks, ior = 1).  Returns rgb8, rgb_f64, the primary hit_id
-        and hit_t, and (rays=True) the primary rays."""
+        and hit_t, and (rays=True) the primary rays, unless `out` (a dict of
+        preallocated buffers: rgb8, rgb_f32, rgb_f64, hit_id, hit_t, rays) is
+        given."""
         cam, lt, p = render_args(camera, light, width, height, spp, rows)
         npx, ns = width * height, width * height * spp
-        out = dict(rgb8=np.zeros((npx, 3), np.uint8), rgb_f64=np.zeros((npx, 3), np.float64),
-                   hit_id=np.zeros(ns, np.int32), hit_t=np.zeros(ns, np.float64))
-        if rays:
-            out["rays"] = np.zeros((ns, 6), np.float64)
-        op = None if optics is None else np.ascontiguousarray(optics, np.float64).reshape(-1, 4)
+        if out is None:
+            out = dict(rgb8=np.zeros((npx, 3), np.uint8), rgb_f64=np.zeros((npx, 3), np.float64),
+                       hit_id=np.zeros(ns, np.int32), hit_t=np.zeros(ns, np.float64))
+            if rays:
+                out["rays"] = np.zeros((ns, 6), np.float64)
+        if optics is None or hasattr(optics, "data_ptr"):
+            op = optics  # None, or a device tensor of num_materials x 4 doubles
+        else:
+            op = np.ascontiguousarray(optics, np.float64).reshape(-1, 4)
         o = _RenderOut(*[_addr(out.get(k)) for k in ("rgb8", "rgb_f32", "hit_id", "hit_t", "shadow", "rays",
                                                      "traversal_stats", "rgb_f64", "depth", "shadow_id")])
         _check(lib().crt_render_recursive(self.h, C.byref(cam), C.byref(lt), C.byref(p), int(depth), _addr(op),

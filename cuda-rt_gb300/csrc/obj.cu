@@ -19,6 +19,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <iterator>
 #include <map>
 #include <sstream>
 #include <string>
@@ -111,24 +112,47 @@ void read_mtl(const std::string& file, std::map<std::string, int>& names, std::v
   }
 }
 
-// One face corner: "v", "v/t", "v//n" or "v/t/n"; indices resolved to 0-based.
-bool corner(const std::string& c, size_t nv, size_t nn, int& vi, int& ni) {
-  const size_t s1 = c.find('/');
-  const std::string vs = c.substr(0, s1);
-  std::string ns;
-  if (s1 != std::string::npos) {
-    const size_t s2 = c.find('/', s1 + 1);
-    if (s2 != std::string::npos) ns = c.substr(s2 + 1);
+// A line of the OBJ as whitespace-separated tokens [b, e) of the file
+// buffer: no allocation per line (a 200,000-face file has a million lines).
+struct Tok {
+  const char* b;
+  const char* e;
+  bool is(const char* w) const {
+    const size_t n = std::strlen(w);
+    return (size_t)(e - b) == n && std::memcmp(b, w, n) == 0;
   }
+  std::string str() const { return std::string(b, e); }
+};
+inline bool space(char c) { return c == ' ' || c == '\t' || c == '\r' || c == '\v' || c == '\f'; }
+
+// A number that fills the token: strtod stops at the first character that is
+// not part of it, which must be the token's end.
+bool tok_double(const Tok& t, double& out) {
   char* e = nullptr;
-  const long v = std::strtol(vs.c_str(), &e, 10);
-  if (vs.empty() || *e != '\0' || v == 0) return false;
+  errno = 0;
+  out = std::strtod(t.b, &e);
+  return e != t.b && e == t.e;
+}
+
+// One face corner: "v", "v/t", "v//n" or "v/t/n"; indices resolved to
+// 0-based (negative ones count back from the current end); ni = -1 when the
+// corner names no normal.
+bool tok_corner(const Tok& t, size_t nv, size_t nn, int& vi, int& ni) {
+  const char* s1 = static_cast<const char*>(std::memchr(t.b, '/', t.e - t.b));
+  const char* ve = s1 ? s1 : t.e;
+  if (ve == t.b) return false;
+  char* e = nullptr;
+  const long v = std::strtol(t.b, &e, 10);
+  if (e != ve || v == 0) return false;
   vi = v > 0 ? (int)(v - 1) : (int)((long)nv + v);
   ni = -1;
-  if (!ns.empty()) {
-    const long n = std::strtol(ns.c_str(), &e, 10);
-    if (*e != '\0' || n == 0) return false;
-    ni = n > 0 ? (int)(n - 1) : (int)((long)nn + n);
+  if (s1) {
+    const char* s2 = static_cast<const char*>(std::memchr(s1 + 1, '/', t.e - (s1 + 1)));
+    if (s2 && s2 + 1 < t.e) {
+      const long n = std::strtol(s2 + 1, &e, 10);
+      if (e != t.e || n == 0) return false;
+      ni = n > 0 ? (int)(n - 1) : (int)((long)nn + n);
+    }
   }
   return true;
 }
@@ -140,38 +164,54 @@ extern "C" {
 crt_status crt_obj_load(const char* obj_path, const char* mtl_dir, crt_obj** out) {
   if (!obj_path || !out) return fail("null argument");
   *out = nullptr;
-  std::ifstream f(obj_path);
+  std::ifstream f(obj_path, std::ios::binary);
   if (!f) return fail(std::string("cannot open ") + obj_path);
+  std::string buf((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
   const std::string base = mtl_dir ? std::string(mtl_dir) : dir_of(obj_path);
   crt_obj* o = new crt_obj;
   std::map<std::string, int> names;
   int cur = -1;
-  std::string line;
   size_t lineno = 0;
-  while (std::getline(f, line)) {
+  std::vector<Tok> t;
+  std::vector<int> cv, cn;
+  const char* p = buf.c_str();
+  const char* const end = p + buf.size();
+  while (p < end) {
+    const char* le = static_cast<const char*>(std::memchr(p, '\n', end - p));
+    if (!le) le = end;
     lineno++;
-    const std::vector<std::string> t = split_ws(line);
-    if (t.empty() || t[0][0] == '#') continue;
-    double x[3];
-    if (t[0] == "v" || t[0] == "vn") {
-      if (!parse3(t, x)) {
+    t.clear();
+    for (const char* q = p; q < le;) {
+      while (q < le && space(*q)) q++;
+      const char* tb = q;
+      while (q < le && !space(*q)) q++;
+      if (q > tb) t.push_back(Tok{tb, q});
+    }
+    p = le + 1;
+    if (t.empty() || *t[0].b == '#') continue;
+    if (t[0].is("v") || t[0].is("vn")) {
+      double x[3];
+      bool ok = t.size() >= 4;
+      for (int k = 0; ok && k < 3; k++) ok = tok_double(t[1 + k], x[k]);
+      if (!ok) {
         delete o;
         return fail("bad vertex at line " + std::to_string(lineno));
       }
-      std::vector<float>& dst = t[0] == "v" ? o->v : o->n;
+      std::vector<float>& dst = t[0].is("v") ? o->v : o->n;
       for (int k = 0; k < 3; k++) dst.push_back((float)x[k]);
-    } else if (t[0] == "mtllib" && t.size() >= 2) {
-      std::string p = base;
-      if (!p.empty() && p.back() != '/') p += '/';
-      read_mtl(p + t[1], names, o->mats, o->ior);
-    } else if (t[0] == "usemtl") {
-      const auto it = t.size() >= 2 ? names.find(t[1]) : names.end();
+    } else if (t[0].is("mtllib") && t.size() >= 2) {
+      std::string mp = base;
+      if (!mp.empty() && mp.back() != '/') mp += '/';
+      read_mtl(mp + t[1].str(), names, o->mats, o->ior);
+    } else if (t[0].is("usemtl")) {
+      const auto it = t.size() >= 2 ? names.find(t[1].str()) : names.end();
       cur = it == names.end() ? -1 : it->second;
-    } else if (t[0] == "f") {
-      std::vector<int> cv, cn;
+    } else if (t[0].is("f")) {
+      cv.clear();
+      cn.clear();
       for (size_t k = 1; k < t.size(); k++) {
         int vi, ni;
-        if (!corner(t[k], o->v.size() / 3, o->n.size() / 3, vi, ni)) {
+        if (!tok_corner(t[k], o->v.size() / 3, o->n.size() / 3, vi, ni)) {
           delete o;
           return fail("bad face corner at line " + std::to_string(lineno));
         }

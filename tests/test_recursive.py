@@ -12,65 +12,9 @@ import numpy as np
 import pytest
 
 
-def _quad(p0, du, dv):
-    p0, du, dv = (np.asarray(x, np.float64) for x in (p0, du, dv))
-    v = np.stack([p0, p0 + du, p0 + du + dv, p0 + dv])
-    n = np.cross(du, dv)
-    n /= np.linalg.norm(n)
-    return v, np.array([[0, 1, 2], [0, 2, 3]]), np.repeat(n[None], 4, 0)
-
-
-def _sphere(center, radius, nu):
-    from crt import data
-    u, tris = data._geodesic(nu)
-    return np.asarray(center) + radius * u, np.asarray(tris), u
-
-
 def optics_scene(emissive=False, nu=6, specular=False):
-    """A floor, a mirror wall behind a glass sphere and a small diffuse
-    sphere, seen from (0, 0, -3).  Materials: 0 floor, 1 mirror, 2 glass, 3
-    diffuse.  Returns (mesh, optics (4, 4): kr xyz + ior).  specular=False
-    leaves ks = 0 (the Phong term's powf is the one operation whose result
-    may differ between CUDA and the host's libm in the last bit)."""
     from crt import data
-    parts = [(_quad((-2, -0.8, -2), (0, 0, 4), (4, 0, 0)), 0),
-             (_quad((-1.5, -0.8, 1.5), (0, 2.3, 0), (3, 0, 0)), 1),
-             (_sphere((0.3, 0.0, 0.0), 0.5, nu), 2),
-             (_sphere((-0.7, -0.45, 0.4), 0.35, max(nu // 2, 1)), 3)]
-    V, T, Nv, mid = [], [], [], []
-    off = 0
-    for (v, t, n), m in parts:
-        V.append(v)
-        Nv.append(n)
-        T.append(t + off)
-        mid.append(np.full(len(t), m, np.int32))
-        off += len(v)
-    cam = (0.0, 0.0, -3.0)
-    v = data.view_transform(np.concatenate(V), cam).astype(np.float32)
-    n = data.view_transform(np.concatenate(Nv), cam, direction=True).astype(np.float32)
-    tris = np.concatenate(T).astype(np.int32)
-    mats = np.zeros((4, 16))
-    ka, kd, ks, kt, ke, sh = slice(0, 3), slice(3, 6), slice(6, 9), slice(9, 12), slice(12, 15), 15
-    if emissive:
-        mats[0, ke] = (0.3, 0.5, 0.2)
-        mats[1, ke] = (0.05, 0.05, 0.1)
-        mats[2, ke] = (0.02, 0.01, 0.0)
-        mats[3, ke] = (0.7, 0.2, 0.1)
-    else:
-        mats[0, kd] = (0.8, 0.7, 0.6)
-        mats[1, kd] = 0.1
-        mats[2, kd] = 0.05
-        mats[3, kd] = (0.2, 0.4, 0.9)
-        if specular:
-            mats[1, ks] = 0.8
-            mats[2, ks] = 0.1
-            mats[3, ks] = 0.3
-    mats[:, sh] = 1.0
-    mats[1, sh] = 20.0
-    mats[2, kt] = (0.9, 0.9, 0.85)
-    optics = np.array([[0, 0, 0, 1.0], [0.8, 0.8, 0.8, 1.0], [0.1, 0.1, 0.1, 1.5], [0, 0, 0, 1.0]])
-    mesh = data.Mesh(v, tris, n, tris.copy(), np.concatenate(mid), mats)
-    return mesh, optics
+    return data.optics_scene(emissive=emissive, nu=nu, specular=specular)
 
 
 def scene_view(aperture=0.0, radius=0.0):
