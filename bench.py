@@ -499,11 +499,16 @@ def run_next_rows(reps=3):
                                                      stream=stream))
         t_d3 = timed(lambda: g_spec.render_recursive(cam, area, W2, H2, spp, 3, d_optics, out={"rgb8": rgb},
                                                      stream=stream))
+        counts = torch.zeros(2, dtype=torch.int64, device="cuda")
+        g_spec.render_recursive(cam, area, W2, H2, spp, 3, d_optics, out={"rgb8": rgb, "traversal_stats": counts},
+                                stream=stream)
+        n_rays, n_shadow = (int(x) for x in counts.cpu().tolist())
         g_lam.check()
         g_spec.check()
         res["recursive"] = {"triangles": spec_mesh.ntri, "image": f"{W2}x{H2}x{spp}spp", "depth": 3,
                             "depth0_ms": round(t_d0, 3), "depth3_ms": round(t_d3, 3),
-                            "primary_mrays_s": round(rays / t_d3 / 1e3, 1)}
+                            "primary_mrays_s": round(rays / t_d3 / 1e3, 1), "rays_traced": n_rays,
+                            "shadow_rays": n_shadow, "all_rays_mrays_s": round((n_rays + n_shadow) / t_d3 / 1e3, 1)}
         # (4) the CLI
         cli = cbuild.build_cli()
         bmp = os.path.join(tmp, "out.bmp")

@@ -476,8 +476,9 @@ crt_status crt_render_recursive(crt_scene* s, const crt_camera* cam, const crt_l
                                 const crt_render_out* o, void* stream) {
   if (!s || !cam || !light || !p || !o) return fail(CRT_INVALID_ARG, "null argument");
   if (depth < 0 || depth > CRT_MAX_DEPTH) return fail(CRT_INVALID_ARG, "depth must be in [0, CRT_MAX_DEPTH]");
-  if (o->traversal_stats || o->shadow || o->shadow_id || o->depth)
-    return fail(CRT_INVALID_ARG, "crt_render_recursive writes rgb8, rgb_f32, rgb_f64, hit_id, hit_t and rays only");
+  if (o->shadow || o->shadow_id || o->depth)
+    return fail(CRT_INVALID_ARG,
+                "crt_render_recursive writes rgb8, rgb_f32, rgb_f64, hit_id, hit_t, rays and traversal_stats only");
   RenderArgs a;
   cudaStream_t st = S(stream);
   if (crt_status e = render_args(s, cam, light, p, st, a)) return e;
@@ -489,7 +490,9 @@ crt_status crt_render_recursive(crt_scene* s, const crt_camera* cam, const crt_l
   const size_t npx = (size_t)p->width * p->height;
   const size_t nsm = npx * (size_t)p->spp;
   const bool band = !(a.row0 == 0 && a.row1 == p->height);
-  DevView v8, vf, vh, vt, vr, vd;
+  DevView v8, vf, vh, vt, vr, vd, vst;
+  CRT_CUDA(vst.open(o->traversal_stats, 2 * sizeof(uint64_t), false, st), "stage stats");
+  if (vst.dev) CRT_CUDA(cudaMemsetAsync(vst.dev, 0, 2 * sizeof(uint64_t), st), "memset");
   CRT_CUDA(v8.open(o->rgb8, 3 * npx, band, st), "stage rgb8");
   CRT_CUDA(vf.open(o->rgb_f32, 3 * sizeof(float) * npx, band, st), "stage rgb_f32");
   CRT_CUDA(vh.open(o->hit_id, sizeof(int32_t) * nsm, band, st), "stage hit_id");
@@ -502,10 +505,12 @@ crt_status crt_render_recursive(crt_scene* s, const crt_camera* cam, const crt_l
   a.hit_t = static_cast<double*>(vt.dev);
   a.rays = static_cast<double*>(vr.dev);
   a.rgbd = static_cast<double*>(vd.dev);
+  a.stats = static_cast<unsigned long long*>(vst.dev);
   CRT_CUDA(launch_render_recursive(dscene(s), a, static_cast<const DOptics*>(vo.dev), depth, st),
            "recursive render launch");
   CRT_CUDA(vo.close(false, st), "unstage");
-  const bool host_out = v8.temp || vf.temp || vh.temp || vt.temp || vr.temp || vd.temp;
+  const bool host_out = v8.temp || vf.temp || vh.temp || vt.temp || vr.temp || vd.temp || vst.temp;
+  CRT_CUDA(vst.close(true, st), "unstage");
   CRT_CUDA(v8.close(true, st), "unstage");
   CRT_CUDA(vf.close(true, st), "unstage");
   CRT_CUDA(vh.close(true, st), "unstage");

@@ -119,6 +119,7 @@ __global__ void __launch_bounds__(128) k_pixels_rec(DScene S, RenderArgs A, cons
   const int gx = (A.W + 15) / 16;
   const D3 lpos = d3(A.lpos[0], A.lpos[1], A.lpos[2]);
   Frame fr[kMaxRecDepth];
+  unsigned long long nrays = 0, nshadow = 0;  // for A.stats
   while (true) {
     int tile = 0;
     if (lane == 0) tile = (int)atomicAdd(A.counter, 1u);
@@ -152,6 +153,7 @@ __global__ void __launch_bounds__(128) k_pixels_rec(DScene S, RenderArgs A, cons
       const int res = traverse<false>(S, rc, rb, h, busy);
       if (res < 0) atomicOr(&S.g->err, kErrStack);
       const bool hit = busy && res > 0;
+      nrays += busy, nshadow += hit;
       if (busy && lvl == 0) {
         const int64_t si = (int64_t)idx * A.spp + k;
         if (A.hit_id) A.hit_id[si] = hit ? h.id : -1;
@@ -257,6 +259,17 @@ __global__ void __launch_bounds__(128) k_pixels_rec(DScene S, RenderArgs A, cons
         if (c > 1) c = 1.0;
         A.rgb8[3 * (int64_t)idx + ch] = (uint8_t)(255.0 * c);
       }
+    }
+  }
+  if (A.stats) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      nrays += __shfl_xor_sync(full, nrays, o);
+      nshadow += __shfl_xor_sync(full, nshadow, o);
+    }
+    if (lane == 0) {
+      atomicAdd(A.stats, nrays);
+      atomicAdd(A.stats + 1, nshadow);
     }
   }
 }

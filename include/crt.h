@@ -170,8 +170,9 @@ crt_status crt_render(crt_scene* scene, const crt_camera* camera, const crt_ligh
  * depth = 0 gives crt_render's image.  optics: num_materials entries (host
  * or device), or NULL for kr = ks (as Scene_h::LoadObj sets it,
  * src/scene.cpp:29) and ior = 1 (tinyobjloader's default).  Writes rgb8,
- * rgb_f32, rgb_f64, and the primary rays' hit_id, hit_t and rays; the
- * other outputs must be NULL. */
+ * rgb_f32, rgb_f64, the primary rays' hit_id, hit_t and rays, and
+ * traversal_stats as [0] rays traced for closest hits (primary, reflected
+ * and refracted), [1] shadow rays; the other outputs must be NULL. */
 #define CRT_MAX_DEPTH 8
 typedef struct crt_optics {
   double kr[3]; /* Material::kr, inc/material.h:16 */

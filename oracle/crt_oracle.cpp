@@ -488,12 +488,14 @@ static V3 shade_hit(const Scene& s, const orc_camera* cam, const orc_light* ligh
 // accepted, |t| < RAY_EPSILON rejected).  optics[4*m]: kr xyz, ior of
 // material m.  Draws from st in the recursion's order (depth first).
 static V3 trace_rec(const Scene& s, const orc_camera* cam, const orc_light* light, const double* optics, V3 org,
-                    V3 dir, int depth, uint32_t& st, int* overflow, Hit* first, int* first_res) {
+                    V3 dir, int depth, uint32_t& st, int* overflow, Hit* first, int* first_res, int64_t* counts) {
   Hit hh;
   int res = traverse(s, org, dir, false, &hh);
   if (res < 0) (*overflow)++;
   if (first) *first = hh, *first_res = res;
+  counts[0]++;
   if (res <= 0) return v3(0.9, 0.9, 0.9);
+  counts[1]++;
   const V3 N = hit_normal(s, hh);
   int sh, shid;
   V3 c = shade_hit(s, cam, light, org, dir, hh, N, st, &sh, &shid, overflow);
@@ -505,7 +507,7 @@ static V3 trace_rec(const Scene& s, const orc_camera* cam, const orc_light* ligh
   if (!(o[0] == 0 && o[1] == 0 && o[2] == 0)) {
     V3 Rdir = (-2.0 * dot(dir, N)) * N + dir;
     Rdir = normalize(Rdir);
-    V3 v = trace_rec(s, cam, light, optics, q, Rdir, depth - 1, st, overflow, nullptr, nullptr);
+    V3 v = trace_rec(s, cam, light, optics, q, Rdir, depth - 1, st, overflow, nullptr, nullptr, counts);
     c = c + mulc(v3(o[0], o[1], o[2]), v);
   }
   if (!(m.kt[0] == 0 && m.kt[1] == 0 && m.kt[2] == 0)) {
@@ -528,7 +530,7 @@ static V3 trace_rec(const Scene& s, const orc_camera* cam, const orc_light* ligh
       const V3 tcos = n * sqrt(TIR);
       V3 Tdir = tcos + tsin;
       Tdir = normalize(Tdir);
-      V3 v = trace_rec(s, cam, light, optics, q, Tdir, depth - 1, st, overflow, nullptr, nullptr);
+      V3 v = trace_rec(s, cam, light, optics, q, Tdir, depth - 1, st, overflow, nullptr, nullptr, counts);
       c = c + mulc(v3(m.kt[0], m.kt[1], m.kt[2]), v);
     }
   }
@@ -739,10 +741,11 @@ int orc_render(void* h, const orc_camera* cam, const orc_light* light, int W, in
 // from the pixel's stream in depth-first order.  optics[4*m] = kr xyz, ior of
 // material m; NULL takes kr = ks (Scene_h::LoadObj sets kr to the MTL's
 // specular colour, src/scene.cpp:29) and ior = 1 (tinyobjloader's default).
-// Outputs as orc_render (hit_id/hit_t: the primary ray's closest hit).
+// Outputs as orc_render (hit_id/hit_t: the primary ray's closest hit);
+// counts[2] (optional): closest-hit rays traced, shadow rays traced.
 int orc_render_rec(void* h, const orc_camera* cam, const orc_light* light, int W, int H, int spp, int depth,
                    const double* optics, uint8_t* rgb8, double* color, int* hit_id, double* hit_t,
-                   const double* rays_in, double* rays_out, int nthreads) {
+                   const double* rays_in, double* rays_out, int nthreads, int64_t* counts) {
   const Scene* s = (const Scene*)h;
   std::vector<double> opt(4 * (size_t)s->nmat);
   for (int m = 0; m < s->nmat; m++) {
@@ -751,13 +754,14 @@ int orc_render_rec(void* h, const orc_camera* cam, const orc_light* light, int W
   }
   const int gx = (W + 15) / 16;
   int overflow = 0;
+  int64_t nrays = 0, nshadow = 0;
   const double invW = 1.0 / double(W), invH = 1.0 / double(H);
   const double aspect = double(W) / double(H);
   const double angle = tan(M_PI * 0.5 * cam->fov / 180.0f);
   const double aperture = 1 / cam->fstop;
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
-#pragma omp parallel for collapse(2) schedule(dynamic, 16) reduction(+ : overflow)
+#pragma omp parallel for collapse(2) schedule(dynamic, 16) reduction(+ : overflow, nrays, nshadow)
 #endif
   for (int py = 0; py < H; py++) {
     for (int px = 0; px < W; px++) {
@@ -786,8 +790,10 @@ int orc_render_rec(void* h, const orc_camera* cam, const orc_light* light, int W
         Hit first;
         int res = 0;
         int ov = 0;
-        acc = acc + trace_rec(*s, cam, light, opt.data(), org, dir, depth, st, &ov, &first, &res);
+        int64_t c[2] = {0, 0};
+        acc = acc + trace_rec(*s, cam, light, opt.data(), org, dir, depth, st, &ov, &first, &res, c);
         overflow += ov;
+        nrays += c[0], nshadow += c[1];
         if (hit_id) hit_id[si] = res > 0 ? first.id : -1;
         if (hit_t) hit_t[si] = res > 0 ? first.t : 0.0;
       }
@@ -804,6 +810,7 @@ int orc_render_rec(void* h, const orc_camera* cam, const orc_light* light, int W
       }
     }
   }
+  if (counts) counts[0] = nrays, counts[1] = nshadow;
   return overflow;
 }
 

@@ -181,10 +181,11 @@ def _render_rec(self, cam, light, width, height, spp, depth, optics=None, rays_i
     f = self.lib.orc_render_rec
     f.restype = C.c_int
     f.argtypes = [C.c_void_p, C.POINTER(_Cam), C.POINTER(_Light), C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p,
-                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+    counts = np.zeros(2, np.int64)
     ov = f(self.h, C.byref(c), C.byref(L), width, height, spp, depth, g(op), rgb.ctypes.data, col.ctypes.data,
-           hid.ctypes.data, ht.ctypes.data, g(ri), g(ro), nthreads)
-    out = dict(rgb=rgb, color=col, hit_id=hid, hit_t=ht, overflow=ov)
+           hid.ctypes.data, ht.ctypes.data, g(ri), g(ro), nthreads, counts.ctypes.data)
+    out = dict(rgb=rgb, color=col, hit_id=hid, hit_t=ht, overflow=ov, counts=counts.tolist())
     if rays_out:
         out["rays"] = ro
     return out

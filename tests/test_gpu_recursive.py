@@ -123,8 +123,26 @@ def test_recursive_rejects_bad_arguments(optics_gpu):
         with pytest.raises(crt.CrtError):
             g.render_recursive(cam, light, 16, 16, 1, depth, optics)
     c, lt, p = crt.render_args(cam, light, 16, 16, 1)
-    stats = np.zeros(2, np.uint64)
-    o = crt._RenderOut(None, None, None, None, None, None, stats.ctypes.data, None, None, None)
+    shadow = np.zeros(16 * 16, np.int32)
+    o = crt._RenderOut(None, None, None, None, shadow.ctypes.data, None, None, None, None, None)
     assert crt.lib().crt_render_recursive(g.h, C.byref(c), C.byref(lt), C.byref(p), 2, None, C.byref(o),
                                           None) == 1
     assert "writes" in crt.lib().crt_last_error_string().decode()
+
+
+@pytest.mark.parametrize("depth", [0, 3])
+def test_recursive_ray_counts(optics_gpu, depth):
+    """traversal_stats of crt_render_recursive counts the rays of every
+    sample's tree and their shadow rays: equal to the oracle's counts."""
+    g, o, optics = optics_gpu
+    cam, light = scene_view()
+    W, H, spp = 40, 32, 3
+    stats = np.zeros(2, np.uint64)
+    out = dict(rgb_f64=np.zeros((W * H, 3)), hit_id=np.zeros(W * H * spp, np.int32), traversal_stats=stats)
+    g.render_recursive(cam, light, W, H, spp, depth, optics, out=out)
+    ref = o.render_recursive(cam, light, W, H, spp, depth, optics)
+    assert_equal(out["rgb_f64"], ref["color"], "colour")
+    assert stats.tolist() == list(ref["counts"])
+    if depth == 0:
+        assert stats[0] == W * H * spp and stats[1] == (out["hit_id"] >= 0).sum()
+
