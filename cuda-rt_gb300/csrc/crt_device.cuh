@@ -398,7 +398,7 @@ __device__ __forceinline__ float entry_bound(int) { return 0.f; }
 
 // Leaf codes carry a flag: bit 30 of ~code set = the leaf's box passed the
 // conservative filter but not the certain one, so its exact box test is
-// still due.  kPop marks "take the next node from the stack".
+// still due (set when the leaf is visited and its triangle is a candidate).  kPop marks "take the next node from the stack".
 constexpr int kLeafBoxDue = 1 << 30;
 constexpr int kLeafIndex = kLeafBoxDue - 1;
 constexpr int kPop = kNoChild;
@@ -429,7 +429,6 @@ __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, const fl
   float tp;
   if (run && !box_cons(r, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5], tp)) run = false;
   int node = S.root;
-  if (node < 0 && !box_sure(r, rb[0], rb[3], rb[1], rb[4], rb[2], rb[5])) node = ~kLeafBoxDue;
   float pb = __int_as_float(0x7f800000);  // prune bound; +inf until a hit
   using E = typename std::conditional<ANY, int, int2>::type;
   TravStack<SHORT, E> stk;
@@ -477,7 +476,6 @@ __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, const fl
           c[k] = __float_as_int(lo.w);
           bool hk = c[k] != kNoChild && box_cons(r, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z, t[k]);
           if (!ANY) hk = hk && !(t[k] > pb);
-          if (hk && c[k] < 0 && !box_sure(r, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z)) c[k] = ~(~c[k] | kLeafBoxDue);
           if (!hk) c[k] = kNoChild;
           if (ANY) t[k] = 0.f;  // pruning bounds are not used
           else if (!hk) t[k] = __int_as_float(0x7f800000);
@@ -511,7 +509,15 @@ __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, const fl
         if (STATS) ts->tris++;
         const float4* lp = reinterpret_cast<const float4*>(S.leaves + (~node & kLeafIndex));
         const float4 a = __ldg(lp), b = __ldg(lp + 1), c = __ldg(lp + 2);
-        if (!tri_reject_sure(r, a, b, c)) cand = node, pending = true;
+        if (!tri_reject_sure(r, a, b, c)) {
+          cand = node, pending = true;
+          // the leaf's box (as the refit computes it from the same vertices)
+          // is tested here rather than when the leaf is pushed: one copy of
+          // the test in the walk's code, and none for leaves never reached
+          if (!box_sure(r, fminf(c.x, fminf(a.x, b.x)), fmaxf(c.x, fmaxf(a.x, b.x)), fminf(c.y, fminf(a.y, b.y)),
+                        fmaxf(c.y, fmaxf(a.y, b.y)), fminf(c.z, fminf(a.z, b.z)), fmaxf(c.z, fmaxf(a.z, b.z))))
+            cand = ~(~cand | kLeafBoxDue);
+        }
         node = kPop;
       }
     }
