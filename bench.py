@@ -47,7 +47,7 @@ W, H, SPP = 1920, 1080, 16
 # Most of these bytes are the lens-table lookups (two random loads per
 # sample, each filling whole L2 lines) and the threads' local memory
 # (traversal stacks and register spills of 155,648 resident threads).
-RENDER_DRAM_BYTES = 10_596_541_696
+RENDER_DRAM_BYTES = 10_521_362_688
 
 
 def peaks():
