@@ -146,3 +146,26 @@ def test_recursive_ray_counts(optics_gpu, depth):
     if depth == 0:
         assert stats[0] == W * H * spp and stats[1] == (out["hit_id"] >= 0).sum()
 
+
+
+@pytest.mark.parametrize("ntri", [0, 1, 2])
+def test_recursive_tiny_scenes(cuda, ntri):
+    """Empty, one- and two-triangle scenes (a leaf root, a single internal
+    node) with a reflecting and transmitting material, depth 4."""
+    import crt
+    from crt import data
+    from oracle.oracle import OracleScene
+    v = np.array([[-1, -1, -3], [1, -1, -3], [0, 1, -3.5], [-1, 0.5, -2.5], [1, 0.5, -2.5], [0, -1, -2]], np.float32)
+    tris = np.array([[0, 1, 2], [3, 4, 5]], np.int32)[:ntri].reshape(-1, 3)
+    n = np.tile(np.array([[0, 0, 1]], np.float32), (6, 1))
+    mats = np.zeros((1, 16))
+    mats[0, 3:6] = 0.4
+    mats[0, 9:12] = 0.5
+    mats[0, 15] = 1.0
+    mesh = data.Mesh(v, tris, n, tris.copy(), np.zeros(ntri, np.int32), mats)
+    optics = np.array([[0.8, 0.7, 0.6, 1.3]])
+    cam, light = scene_view()
+    out = crt.Scene(mesh).render_recursive(cam, light, 24, 16, 2, 4, optics)
+    ref = OracleScene(mesh).render_recursive(cam, light, 24, 16, 2, 4, optics)
+    assert_equal(out["rgb_f64"], ref["color"], "colour")
+    assert_equal(out["hit_id"], ref["hit_id"], "hit id")
