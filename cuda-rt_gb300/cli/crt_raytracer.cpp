@@ -1,7 +1,8 @@
 // crt_raytracer -- drop-in for the reference's cuda_bvh executable
 // (src/main.cpp:91-332): the same flags and defaults, an OBJ/MTL scene in, a
-// 24-bit BMP out, rendered by libcrt (crt_obj_load -> crt_scene_create ->
-// crt_render, or crt_render_recursive with --depth, -> crt_write_bmp).
+// 24-bit BMP out, through the reference's call sequence on crt::RayTracer
+// (include/crt.hpp): LoadObj, setHostLight, setCamera, setUpDevice, run,
+// pullRaytracedImage, writeImage.
 //
 //   -i, --input <file.obj>         scene (required); its MTL is read from the
 //                                  OBJ's directory, as main.cpp passes it
@@ -34,7 +35,7 @@
 #include <string>
 #include <vector>
 
-#include "crt.h"
+#include "crt.hpp"
 
 namespace {
 
@@ -79,21 +80,14 @@ bool scalar(const std::string& s, double& out) {
   return end != s.c_str();
 }
 
-int die(const char* what) {
-  std::fprintf(stderr, "crt_raytracer: %s: %s\n", what, crt_last_error_string());
-  return 1;
-}
-
 }  // namespace
 
 int main(int argc, char** argv) {
   std::string input, output;
   int width = 512, height = 512, spp = 20, depth = 0;
-  crt_camera cam{};
-  cam.fov = 30.0, cam.fstop = 8.0, cam.focal_point = 10.0;  // Camera::Camera (kernels/camera.cu:10-22)
-  crt_light light{};
-  for (int k = 0; k < 3; k++) light.color[k] = 1.0, light.position[k] = 1.0;  // Light_h::Light_h (inc/Light.h)
-  light.radius = 0.5, light.constant_term = 0.0, light.linear_term = 0.01, light.quadratic_term = 0.001;
+  crt::Camera camera;  // fov 30, f-stop 8, focal point 10 (kernels/camera.cu:10-22)
+  crt::Light_h light;  // position and colour (1,1,1), radius 0.5, falloff (0, 0.01, 0.001) (inc/Light.h:28)
+  double fov = camera.getFOV(), fstop = 1 / camera.getAperature(), focal = camera.getFocalPoint();
   if (argc <= 1) {
     usage();
     return 0;
@@ -146,22 +140,22 @@ int main(int argc, char** argv) {
       ok = end != val.c_str() && *end == '\0' && x >= 0 && x <= CRT_MAX_DEPTH;
       depth = (int)x;
     } else if (name == "fstop") {
-      ok = scalar(val, cam.fstop);
+      ok = scalar(val, fstop);
     } else if (name == "fov") {
-      ok = scalar(val, cam.fov);
+      ok = scalar(val, fov);
     } else if (name == "focalpoint") {
-      ok = scalar(val, cam.focal_point);
+      ok = scalar(val, focal);
     } else if (name == "radius") {
       ok = scalar(val, light.radius);
     } else if (name == "position" || name == "color") {
       ok = vec3(val, v);
-      double* dst = name == "position" ? light.position : light.color;
-      for (int k = 0; ok && k < 3; k++) dst[k] = v[k];
+      if (ok) (name == "position" ? light.position : light.color) = crt::Vec3d{v[0], v[1], v[2]};
     } else if (name == "attenuation") {
       ok = vec3(val, v);
-      if (ok) light.constant_term = v[0], light.linear_term = v[1], light.quadratic_term = v[2];
+      if (ok) light.constantTerm = v[0], light.linearTerm = v[1], light.quadraticTerm = v[2];
     } else if (name == "orientation") {
       ok = vec3(val, v);  // unused by the positional light
+      if (ok) light.orientation = crt::Vec3d{v[0], v[1], v[2]};
     }  // numeric / nonempty: accepted and ignored
     if (!ok) {
       std::fprintf(stderr, "crt_raytracer: bad value '%s' for --%s\n", val.c_str(), o->l);
@@ -172,30 +166,25 @@ int main(int argc, char** argv) {
     std::fprintf(stderr, "crt_raytracer: an input OBJ (-i) is required\n");
     return 1;
   }
-  crt_obj* obj = nullptr;
-  if (crt_obj_load(input.c_str(), nullptr, &obj) != CRT_OK) return die("loading the scene");
-  crt_mesh_desc desc;
-  crt_obj_mesh(obj, &desc);
-  crt_scene* scene = nullptr;
-  if (crt_scene_create(&desc, nullptr, &scene) != CRT_OK) return die("building the scene");
-  std::vector<uint8_t> rgb((size_t)width * height * 3);
-  crt_render_params params{width, height, spp, 0, 0};
-  crt_render_out out{};
-  out.rgb8 = rgb.data();
-  if (depth == 0) {
-    if (crt_render(scene, &cam, &light, &params, &out, nullptr) != CRT_OK) return die("rendering");
-  } else {
-    std::vector<crt_optics> optics((size_t)desc.num_materials);
-    crt_obj_optics(obj, optics.data());
-    if (crt_render_recursive(scene, &cam, &light, &params, depth, optics.data(), &out, nullptr) != CRT_OK)
-      return die("rendering");
+  camera.setfov(fov);
+  camera.setFstop(fstop);
+  camera.setFocalPoint(focal);
+  try {
+    crt::RayTracer rayTracer(width, height, 1);
+    rayTracer.setSamples(spp);
+    rayTracer.setDepth(depth);
+    rayTracer.LoadObj(input, "");  // the MTL is read from the OBJ's directory
+    rayTracer.setHostLight(light);
+    rayTracer.setCamera(&camera);
+    rayTracer.setUpDevice();
+    rayTracer.run();
+    rayTracer.pullRaytracedImage();
+    if (!output.empty()) rayTracer.writeImage(output);
+    std::printf("crt_raytracer: %d triangles, %dx%d, %d spp, depth %d -> %s\n", rayTracer.scene().numTriangles(),
+                width, height, spp, depth, output.empty() ? "(no output)" : output.c_str());
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "crt_raytracer: %s\n", e.what());
+    return 1;
   }
-  if (crt_scene_check(scene, nullptr) != CRT_OK) return die("rendering");
-  if (!output.empty() && crt_write_bmp(output.c_str(), width, height, rgb.data()) != CRT_OK)
-    return die("writing the image");
-  std::printf("crt_raytracer: %d triangles, %dx%d, %d spp -> %s\n", desc.num_triangles, width, height, spp,
-              output.empty() ? "(no output)" : output.c_str());
-  crt_scene_destroy(scene);
-  crt_obj_free(obj);
   return 0;
 }

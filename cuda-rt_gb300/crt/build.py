@@ -79,7 +79,7 @@ def build_cli() -> str:
     """The drop-in command-line renderer (cli/crt_raytracer.cpp), linked
     against libcrt.so next to it."""
     src = os.path.join(CLI_DIR, "crt_raytracer.cpp")
-    if _stale(CLI, [src, LIB, os.path.join(INCLUDE, "crt.h")]):
+    if _stale(CLI, [src, LIB, os.path.join(INCLUDE, "crt.h"), os.path.join(INCLUDE, "crt.hpp")]):
         subprocess.check_call(["g++", "-O2", "-std=c++17", "-I", INCLUDE, src, "-L", LIBDIR, "-lcrt",
                                "-Wl,-rpath,$ORIGIN", "-o", CLI])
     return CLI

@@ -37,3 +37,38 @@ def test_library_is_in_tree_and_built_for_sm103a(built):
     assert os.path.exists(b.LIB) and b.LIB.startswith(ROOT)
     assert "arch=compute_103a,code=sm_103a" in " ".join(b.ARCH)
     assert "-fmad=false" in b.FLAGS
+
+
+def test_cpp_wrappers_compile_and_link(built, tmp_path):
+    """include/crt.hpp (Camera, Light_h, Scene, BVH, RayTracer with the
+    reference's method names) compiles warning-free and links against the
+    library; a program using it reports a missing OBJ as crt::Error."""
+    import subprocess
+    src = tmp_path / "use.cpp"
+    src.write_text(r'''
+#include "crt.hpp"
+#include <cstdio>
+int main() {
+  crt::Camera cam;
+  cam.setfov(45); cam.setFstop(16); cam.setFocalPoint(2);
+  if (cam.getFOV() != 45 || cam.getAperature() != 1.0 / 16 || cam.getFocalPoint() != 2) return 2;
+  crt::Light_h light;
+  if (light.radius != 0.5 || light.linearTerm != 0.01) return 3;
+  crt::RayTracer rt(64, 32, 1);
+  rt.setCamera(&cam);
+  rt.setHostLight(light);
+  try {
+    rt.LoadObj("/nonexistent/scene.obj", "");
+  } catch (const crt::Error& e) {
+    std::printf("%d %s\n", (int)e.status, e.what());
+    return e.status == CRT_INVALID_ARG ? 0 : 4;
+  }
+  return 5;
+}
+''')
+    lib = os.path.join(ROOT, "cuda-rt_gb300", "lib")
+    exe = str(tmp_path / "use")
+    subprocess.check_call(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                           str(src), "-L", lib, "-lcrt", "-Wl,-rpath," + lib, "-o", exe])
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "cannot open" in r.stdout, (r.returncode, r.stdout, r.stderr)
