@@ -150,3 +150,64 @@ def test_cli_depth_reflections_and_refractions(cli_scene, tmp_path):
     r = subprocess.run([cli, "-i", obj, "--depth", "9"], capture_output=True, text=True, timeout=60)
     assert r.returncode != 0 and "bad value" in r.stderr
 
+
+
+def test_cpp_bvh_intersect_matches_oracle(cli_scene, tmp_path):
+    """crt::Scene + crt::BVH (include/crt.hpp): BVH_d::intersect and
+    intersectAny on random rays through the C++ classes, against the oracle."""
+    from oracle.oracle import OracleScene
+    cli, d, obj, mesh = cli_scene
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "bvh.cpp"
+    src.write_text(r'''
+#include "crt.hpp"
+#include <cstdio>
+#include <vector>
+int main(int argc, char** argv) {
+  crt::Scene scene;
+  scene.LoadObj(argv[1]);
+  scene.setUpDevice();
+  crt::BVH bvh(scene);
+  bvh.setUp();
+  FILE* f = std::fopen(argv[2], "rb");
+  std::vector<double> rays;
+  double x;
+  while (std::fread(&x, sizeof x, 1, f) == 1) rays.push_back(x);
+  std::fclose(f);
+  const long n = (long)rays.size() / 6;
+  std::vector<int> ids(n), any(n);
+  std::vector<double> t(n), ta(n);
+  bvh.intersect(rays.data(), n, ids.data(), t.data());
+  bvh.intersectAny(rays.data(), n, any.data(), ta.data());
+  f = std::fopen(argv[3], "wb");
+  std::fwrite(ids.data(), sizeof(int), n, f);
+  std::fwrite(t.data(), sizeof(double), n, f);
+  std::fwrite(any.data(), sizeof(int), n, f);
+  std::fclose(f);
+  return 0;
+}
+''')
+    lib = os.path.join(root, "cuda-rt_gb300", "lib")
+    exe = str(tmp_path / "bvh")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", os.path.join(root, "include"), str(src), "-L", lib,
+                           "-lcrt", "-Wl,-rpath," + lib, "-o", exe])
+    rng = np.random.default_rng(5)
+    n = 4096
+    org = rng.uniform(-0.3, 0.3, (n, 3))
+    target = mesh.verts[rng.integers(0, len(mesh.verts), n)].astype(np.float64) + rng.normal(0, 0.002, (n, 3))
+    dirs = target - org
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    rays = np.concatenate([org, dirs], 1)
+    rays.astype(np.float64).tofile(str(tmp_path / "rays.bin"))
+    subprocess.run([exe, obj, str(tmp_path / "rays.bin"), str(tmp_path / "out.bin")], check=True, timeout=120)
+    raw = open(tmp_path / "out.bin", "rb").read()
+    ids = np.frombuffer(raw[:4 * n], np.int32)
+    t = np.frombuffer(raw[4 * n:12 * n], np.float64)
+    anyh = np.frombuffer(raw[12 * n:16 * n], np.int32)
+    o = OracleScene(mesh)
+    rid, rt, _ = o.trace(rays)
+    aid, _, _ = o.trace(rays, any_hit=True)
+    assert_equal(ids, rid, "closest ids")
+    assert_equal(t, rt, "closest t")
+    assert_equal(anyh, aid, "any-hit ids")
+    assert (ids >= 0).sum() > n // 8
