@@ -87,6 +87,7 @@ def lib():
         vp, i32, i64 = C.c_void_p, C.c_int32, C.c_int64
         sig = {
             "crt_scene_create": [vp, vp, vp],
+            "crt_scene_create_borrowed": [vp, vp, vp],
             "crt_scene_destroy": [vp],
             "crt_scene_set_vertices": [vp, vp, C.c_int, vp],
             "crt_bvh_build": [vp, vp],
@@ -153,9 +154,12 @@ def _stream(stream):
 
 
 class Scene:
-    """Scene_d + BVH_d: a mesh on the GPU with its LBVH (built on construction)."""
+    """Scene_d + BVH_d: a mesh on the GPU with its LBVH (built on construction).
+    borrow=True (crt_scene_create_borrowed): the mesh's arrays are CUDA
+    tensors that the scene uses in place (kept referenced here); rewrite the
+    vertex tensor and call set_vertices(None, rebuild) to refit from it."""
 
-    def __init__(self, mesh, stream=None):
+    def __init__(self, mesh, stream=None, borrow=False):
         self._keep = []
 
         def hold(a, dt):
@@ -166,7 +170,9 @@ class Scene:
             self._keep.append(a)
             return _addr(a)
 
-        mats = np.ascontiguousarray(np.asarray(mesh.materials, np.float64).reshape(-1, 16))
+        mats = mesh.materials
+        if not hasattr(mats, "data_ptr"):  # device tensors are passed as they are
+            mats = np.ascontiguousarray(np.asarray(mats, np.float64).reshape(-1, 16))
         self.ntri = int(mesh.vidx.shape[0])
         self.nv = int(mesh.verts.shape[0])
         self.nmat = int(mats.shape[0])
@@ -174,9 +180,11 @@ class Scene:
                       int(mesh.normals.shape[0]), hold(mesh.vidx, np.int32), hold(mesh.nidx, np.int32), self.ntri,
                       hold(mats, np.float64), int(mats.shape[0]), hold(mesh.matid, np.int32))
         h = C.c_void_p()
-        _check(lib().crt_scene_create(C.byref(d), _stream(stream), C.byref(h)))
+        create = lib().crt_scene_create_borrowed if borrow else lib().crt_scene_create
+        _check(create(C.byref(d), _stream(stream), C.byref(h)))
         self.h = h
-        self._keep = []
+        if not borrow:
+            self._keep = []
 
     def close(self):
         if getattr(self, "h", None):
@@ -190,6 +198,7 @@ class Scene:
             pass
 
     def set_vertices(self, verts, rebuild: bool, stream=None):
+        """New vertex positions (None: a borrowing scene re-reads its own)."""
         if isinstance(verts, np.ndarray):
             verts = np.ascontiguousarray(verts, np.float32)
         _check(lib().crt_scene_set_vertices(self.h, _addr(verts), int(bool(rebuild)), _stream(stream)))

@@ -1127,6 +1127,31 @@ cudaError_t launch_build_batch(const BatchBufs& b, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// Index arrays that came from device memory (the host checks the others):
+// every vertex, normal and material index in range, or kErrIndex.  Reads
+// only the index arrays, so a bad index is reported before any kernel uses
+// it to address the vertices.
+__global__ void __launch_bounds__(256) k_check_indices(const int* __restrict__ vidx, const int* __restrict__ nidx,
+                                                       const int* __restrict__ matid, int n, int nv, int nn, int nm,
+                                                       SceneGlobals* g) {
+  bool bad = false;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 3 * (int64_t)n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int v = __ldg(vidx + i), k = __ldg(nidx + i);
+    bad = bad || (unsigned)v >= (unsigned)nv || (unsigned)k >= (unsigned)nn;
+    if (i < n) bad = bad || (unsigned)__ldg(matid + i) >= (unsigned)nm;
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(&g->err, kErrIndex);
+}
+
+cudaError_t launch_check_indices(const MeshBufs& m, const BuildBufs& b, cudaStream_t st) {
+  if (m.ntri <= 0) return cudaSuccess;
+  const int64_t need = (3 * (int64_t)m.ntri + 255) / 256;
+  const int grid = (int)(need < (int64_t)num_sms() * 8 ? need : (int64_t)num_sms() * 8);
+  k_check_indices<<<grid, 256, 0, st>>>(m.vidx, m.nidx, m.matid, m.ntri, m.nv, m.nn, m.nmat, b.g);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_refit(const MeshBufs& m, const BuildBufs& b, cudaStream_t st) {
   const int n = m.ntri;
   if (n <= 0) return cudaSuccess;

@@ -16,6 +16,10 @@ struct crt_scene {
   MeshBufs m;
   BuildBufs b;
   bool built = false;
+  // borrowing scene (crt_scene_create_borrowed): m's arrays are the caller's,
+  // except a material-id array of zeros allocated when none was given
+  bool borrowed = false;
+  int* own_matid = nullptr;
   unsigned* counter = nullptr;
   void* block = nullptr;  // one allocation backing the build arrays
   size_t block_bytes = 0;
@@ -112,17 +116,21 @@ crt_status check_globals(crt_scene* s, cudaStream_t st) {
   CRT_CUDA(cudaMemcpy(&err, &s->b.g->err, sizeof(int), cudaMemcpyDeviceToHost), "read error flags");
   if (err & kErrTimeout) return fail(CRT_TIMEOUT, "a radix-sort look-back wait timed out");
   if (err & kErrStack) return fail(CRT_STACK_OVERFLOW, "a traversal exceeded the 64-entry stack");
+  if (err & kErrIndex) return fail(CRT_INVALID_ARG, "a vertex, normal or material index is out of range");
   if (err & kErrNonFinite) return fail(CRT_INVALID_ARG, "non-finite (or |x| > 1e37) vertex coordinate");
   return CRT_OK;
 }
 
 void free_scene(crt_scene* s) {
-  cudaFree(s->m.verts);
-  cudaFree(s->m.normals);
-  cudaFree(s->m.vidx);
-  cudaFree(s->m.nidx);
-  cudaFree(s->m.matid);
-  cudaFree(s->m.mats);
+  if (!s->borrowed) {
+    cudaFree(s->m.verts);
+    cudaFree(s->m.normals);
+    cudaFree(s->m.vidx);
+    cudaFree(s->m.nidx);
+    cudaFree(s->m.matid);
+    cudaFree(s->m.mats);
+  }
+  cudaFree(s->own_matid);
   cudaFree(s->block);
   cudaFree(s->counter);
 }
@@ -139,7 +147,10 @@ extern "C" {
 const char* crt_last_error_string(void) { return g_err.c_str(); }
 const char* crt_version(void) { return "cuda-rt-gb300 0.1 (sm_103a)"; }
 
-crt_status crt_scene_create(const crt_mesh_desc* d, void* stream, crt_scene** out) {
+// crt_scene_create and crt_scene_create_borrowed: checks, device arrays
+// (copies, or the caller's own when borrowing), build arrays, index checks of
+// device-resident indices, then the build.
+static crt_status create_scene(const crt_mesh_desc* d, void* stream, bool borrow, crt_scene** out) {
   if (!d || !out) return fail(CRT_INVALID_ARG, "null argument");
   *out = nullptr;
   const int n = d->num_triangles;
@@ -149,7 +160,13 @@ crt_status crt_scene_create(const crt_mesh_desc* d, void* stream, crt_scene** ou
     return fail(CRT_INVALID_ARG, "triangles need vertices and vertex_indices");
   if (n > 0 && (!d->normals || d->num_normals <= 0)) return fail(CRT_INVALID_ARG, "normals are required");
   if (!d->materials || d->num_materials <= 0) return fail(CRT_INVALID_ARG, "at least one material is required");
-  // Index checks when the indices are host memory.
+  if (borrow) {
+    const void* arrays[6] = {d->vertices, d->normals, d->vertex_indices, d->normal_indices, d->materials,
+                             d->material_ids};
+    for (const void* p : arrays)
+      if (p && !is_device_ptr(p)) return fail(CRT_INVALID_ARG, "a borrowing scene takes device pointers only");
+  }
+  // Index checks when the indices are host memory (device ones: k_check_indices).
   if (n > 0 && !is_device_ptr(d->vertex_indices)) {
     for (int64_t i = 0; i < 3 * (int64_t)n; i++)
       if (d->vertex_indices[i] < 0 || d->vertex_indices[i] >= d->num_vertices)
@@ -180,12 +197,27 @@ crt_status crt_scene_create(const crt_mesh_desc* d, void* stream, crt_scene** ou
 #define ALLOC(ptr, bytes)                                                 \
   if ((bytes) > 0 && (e = cudaMalloc(&(ptr), (bytes))) != cudaSuccess) \
     return bail(e, "cudaMalloc");
-  ALLOC(m.verts, sizeof(float) * 3 * (size_t)m.nv);
-  ALLOC(m.normals, sizeof(float) * 3 * (size_t)m.nn);
-  ALLOC(m.vidx, sizeof(int) * 3 * (size_t)n);
-  ALLOC(m.nidx, sizeof(int) * 3 * (size_t)n);
-  ALLOC(m.matid, sizeof(int) * (size_t)n);
-  ALLOC(m.mats, sizeof(DMat) * (size_t)m.nmat);
+  s->borrowed = borrow;
+  if (borrow) {
+    m.verts = const_cast<float*>(d->vertices);
+    m.normals = const_cast<float*>(d->normals);
+    m.vidx = const_cast<int*>(d->vertex_indices);
+    m.nidx = const_cast<int*>(d->normal_indices ? d->normal_indices : d->vertex_indices);
+    m.mats = reinterpret_cast<DMat*>(const_cast<crt_material*>(d->materials));
+    if (d->material_ids) {
+      m.matid = const_cast<int*>(d->material_ids);
+    } else {
+      ALLOC(s->own_matid, sizeof(int) * (size_t)(n > 0 ? n : 1));
+      m.matid = s->own_matid;
+    }
+  } else {
+    ALLOC(m.verts, sizeof(float) * 3 * (size_t)m.nv);
+    ALLOC(m.normals, sizeof(float) * 3 * (size_t)m.nn);
+    ALLOC(m.vidx, sizeof(int) * 3 * (size_t)n);
+    ALLOC(m.nidx, sizeof(int) * 3 * (size_t)n);
+    ALLOC(m.matid, sizeof(int) * (size_t)n);
+    ALLOC(m.mats, sizeof(DMat) * (size_t)m.nmat);
+  }
   ALLOC(s->counter, sizeof(unsigned) * 4);
   // build arrays, one block
   BuildBufs& b = s->b;
@@ -222,19 +254,33 @@ crt_status crt_scene_create(const crt_mesh_desc* d, void* stream, crt_scene** ou
   auto up = [&](void* dst, const void* src, size_t bytes) {
     return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, st) : cudaSuccess;
   };
-  if ((e = up(m.verts, d->vertices, sizeof(float) * 3 * (size_t)m.nv)) != cudaSuccess) return bail(e, "upload");
-  if ((e = up(m.normals, d->normals, sizeof(float) * 3 * (size_t)m.nn)) != cudaSuccess) return bail(e, "upload");
-  if ((e = up(m.vidx, d->vertex_indices, sizeof(int) * 3 * (size_t)n)) != cudaSuccess) return bail(e, "upload");
-  if ((e = up(m.nidx, d->normal_indices ? d->normal_indices : d->vertex_indices, sizeof(int) * 3 * (size_t)n)) !=
-      cudaSuccess)
-    return bail(e, "upload");
-  if (d->material_ids) {
-    if ((e = up(m.matid, d->material_ids, sizeof(int) * (size_t)n)) != cudaSuccess) return bail(e, "upload");
-  } else if (n > 0 && (e = cudaMemsetAsync(m.matid, 0, sizeof(int) * (size_t)n, st)) != cudaSuccess) {
-    return bail(e, "memset");
-  }
   static_assert(sizeof(DMat) == sizeof(crt_material), "material layout");
-  if ((e = up(m.mats, d->materials, sizeof(DMat) * (size_t)m.nmat)) != cudaSuccess) return bail(e, "upload");
+  if (!borrow) {
+    if ((e = up(m.verts, d->vertices, sizeof(float) * 3 * (size_t)m.nv)) != cudaSuccess) return bail(e, "upload");
+    if ((e = up(m.normals, d->normals, sizeof(float) * 3 * (size_t)m.nn)) != cudaSuccess) return bail(e, "upload");
+    if ((e = up(m.vidx, d->vertex_indices, sizeof(int) * 3 * (size_t)n)) != cudaSuccess) return bail(e, "upload");
+    if ((e = up(m.nidx, d->normal_indices ? d->normal_indices : d->vertex_indices, sizeof(int) * 3 * (size_t)n)) !=
+        cudaSuccess)
+      return bail(e, "upload");
+    if (d->material_ids && (e = up(m.matid, d->material_ids, sizeof(int) * (size_t)n)) != cudaSuccess)
+      return bail(e, "upload");
+    if ((e = up(m.mats, d->materials, sizeof(DMat) * (size_t)m.nmat)) != cudaSuccess) return bail(e, "upload");
+  }
+  if (!d->material_ids && n > 0 && (e = cudaMemsetAsync(m.matid, 0, sizeof(int) * (size_t)n, st)) != cudaSuccess)
+    return bail(e, "memset");
+  // device-resident indices are checked on the device before the build reads them
+  const bool dev_idx = n > 0 && (is_device_ptr(d->vertex_indices) || (d->normal_indices && is_device_ptr(d->normal_indices)) ||
+                                 (d->material_ids && is_device_ptr(d->material_ids)));
+  if (dev_idx) {
+    if ((e = launch_check_indices(m, b, st)) != cudaSuccess) return bail(e, "index check launch");
+    crt_status r = check_globals(s, st);
+    if (r != CRT_OK) {
+      std::string msg = g_err;
+      free_scene(s);
+      delete s;
+      return fail(r, msg);
+    }
+  }
   if ((e = launch_build(m, b, st)) != cudaSuccess) return bail(e, "build launch");
   s->built = true;
   crt_status r = check_globals(s, st);
@@ -248,6 +294,14 @@ crt_status crt_scene_create(const crt_mesh_desc* d, void* stream, crt_scene** ou
   return CRT_OK;
 }
 
+crt_status crt_scene_create(const crt_mesh_desc* d, void* stream, crt_scene** out) {
+  return create_scene(d, stream, false, out);
+}
+
+crt_status crt_scene_create_borrowed(const crt_mesh_desc* d, void* stream, crt_scene** out) {
+  return create_scene(d, stream, true, out);
+}
+
 crt_status crt_scene_destroy(crt_scene* s) {
   if (!s) return CRT_OK;
   cudaDeviceSynchronize();
@@ -257,9 +311,12 @@ crt_status crt_scene_destroy(crt_scene* s) {
 }
 
 crt_status crt_scene_set_vertices(crt_scene* s, const float* v, int rebuild, void* stream) {
-  if (!s || (!v && s->m.nv > 0)) return fail(CRT_INVALID_ARG, "null argument");
+  if (!s) return fail(CRT_INVALID_ARG, "null scene");
+  if (s->borrowed && v)
+    return fail(CRT_INVALID_ARG, "a borrowing scene reads the caller's vertex array: update it in place, pass NULL");
+  if (!s->borrowed && !v && s->m.nv > 0) return fail(CRT_INVALID_ARG, "null argument");
   cudaStream_t st = S(stream);
-  if (s->m.nv > 0)
+  if (!s->borrowed && s->m.nv > 0)
     CRT_CUDA(cudaMemcpyAsync(s->m.verts, v, sizeof(float) * 3 * (size_t)s->m.nv, cudaMemcpyDefault, st), "upload");
   if (rebuild || !s->built) {
     CRT_CUDA(launch_build(s->m, s->b, st), "build launch");
@@ -523,6 +580,7 @@ crt_status crt_render_recursive(crt_scene* s, const crt_camera* cam, const crt_l
 
 crt_status crt_scene_set_materials(crt_scene* s, const crt_material* mats, int32_t num, void* stream) {
   if (!s || !mats) return fail(CRT_INVALID_ARG, "null argument");
+  if (s->borrowed) return fail(CRT_INVALID_ARG, "a borrowing scene reads the caller's material array");
   if (num != s->m.nmat) return fail(CRT_INVALID_ARG, "material count differs from the scene's");
   CRT_CUDA(cudaMemcpyAsync(s->m.mats, mats, sizeof(DMat) * (size_t)num, cudaMemcpyDefault, S(stream)), "upload");
   return CRT_OK;

@@ -69,6 +69,7 @@ enum : int {
   kErrNonFinite = 1,
   kErrTimeout = 2,
   kErrStack = 4,
+  kErrIndex = 8,  // a vertex, normal or material index out of range
 };
 
 // Everything a traversal needs, passed by value.

@@ -69,6 +69,8 @@ cudaError_t launch_build_batch(const BatchBufs& b, cudaStream_t st);
 // build.cu
 cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st);
 cudaError_t launch_refit(const MeshBufs& m, const BuildBufs& b, cudaStream_t st);
+// Range checks of device-resident index arrays (kErrIndex in b.g->err).
+cudaError_t launch_check_indices(const MeshBufs& m, const BuildBufs& b, cudaStream_t st);
 cudaError_t launch_morton(const float* verts, const int* vidx, int n, const float* box6, uint32_t* codes,
                           cudaStream_t st);
 // Stable LSD radix sort; scratch holds sort_scratch_bytes(n, key_bits).

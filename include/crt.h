@@ -112,8 +112,18 @@ typedef struct crt_render_out {
 
 /* ---- scene lifetime: Scene_d::operator=(const Scene_h&) (src/scene.cpp:82-160)
  * uploads the mesh and builds the BVH; ~Scene_d (src/scene.cpp:163-171) frees.
- * crt_scene_create does both steps and synchronises `stream`. */
+ * crt_scene_create does both steps and synchronises `stream`.  The mesh arrays
+ * may be host or device memory; the scene keeps its own copies.  Index arrays
+ * in device memory are range-checked on the device before the build. */
 crt_status crt_scene_create(const crt_mesh_desc* mesh, void* stream, crt_scene** out);
+/* The same with the caller's device arrays borrowed, not copied: every array
+ * of `mesh` must be device memory and stay valid, unchanged except as below,
+ * until crt_scene_destroy (NULL normal_indices: the vertex indices index the
+ * normals; NULL material_ids: material 0, in an array the scene allocates).
+ * Vertices may be rewritten in place between calls; then
+ * crt_scene_set_vertices(scene, NULL, rebuild, stream) refits or rebuilds
+ * from them (a non-NULL array is refused, as is crt_scene_set_materials). */
+crt_status crt_scene_create_borrowed(const crt_mesh_desc* mesh, void* stream, crt_scene** out);
 crt_status crt_scene_destroy(crt_scene* scene);
 
 /* New vertex positions for the same triangles (num_vertices * 3 floats),
