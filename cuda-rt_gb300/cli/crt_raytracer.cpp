@@ -18,6 +18,8 @@
 //   -d, --orientation x,y,z        accepted; a positional light ignores it
 //   -n, --numeric, -1, --nonempty  accepted and ignored, as in main.cpp
 //       --spp <int>                samples per pixel (default 20, the reference's N)
+//       --seed <int>               0 (default): the reference's random streams; other
+//                                  values give an independent render
 //       --depth <int>              levels of reflected and refracted rays (default 0:
 //                                  the reference's image, whose traceRay block for
 //                                  them is commented out; at most CRT_MAX_DEPTH),
@@ -49,13 +51,13 @@ const Opt kOpts[] = {{'i', "input", true},       {'o', "output", true},      {'w
                      {'P', "focalpoint", true},  {'p', "position", true},    {'c', "color", true},
                      {'a', "attenuation", true}, {'R', "radius", true},      {'d', "orientation", true},
                      {'n', "numeric", true},     {'1', "nonempty", true},    {0, "spp", true},
-                     {0, "depth", true},         {0, "help", false}};
+                     {0, "depth", true},         {0, "seed", true},          {0, "help", false}};
 
 void usage() {
   std::printf(
       "USAGE: crt_raytracer -i scene.obj -o image.bmp [-w W] [-h H] [-f fstop] [-v fov] [-P focal]\n"
       "                     [-p x,y,z] [-c r,g,b] [-a a,b,c] [-R radius] [-d x,y,z] [--spp N]\n"
-      "                     [--depth N]\n");
+      "                     [--depth N] [--seed N]\n");
 }
 
 bool vec3(const std::string& s, double out[3]) {
@@ -85,6 +87,7 @@ bool scalar(const std::string& s, double& out) {
 int main(int argc, char** argv) {
   std::string input, output;
   int width = 512, height = 512, spp = 20, depth = 0;
+  unsigned long seed = 0;
   crt::Camera camera;  // fov 30, f-stop 8, focal point 10 (kernels/camera.cu:10-22)
   crt::Light_h light;  // position and colour (1,1,1), radius 0.5, falloff (0, 0.01, 0.001) (inc/Light.h:28)
   double fov = camera.getFOV(), fstop = 1 / camera.getAperature(), focal = camera.getFocalPoint();
@@ -139,6 +142,10 @@ int main(int argc, char** argv) {
       const long x = std::strtol(val.c_str(), &end, 10);
       ok = end != val.c_str() && *end == '\0' && x >= 0 && x <= CRT_MAX_DEPTH;
       depth = (int)x;
+    } else if (name == "seed") {
+      char* end = nullptr;
+      seed = std::strtoul(val.c_str(), &end, 10);
+      ok = end != val.c_str() && *end == '\0' && seed <= 0xFFFFFFFFul;
     } else if (name == "fstop") {
       ok = scalar(val, fstop);
     } else if (name == "fov") {
@@ -173,6 +180,7 @@ int main(int argc, char** argv) {
     crt::RayTracer rayTracer(width, height, 1);
     rayTracer.setSamples(spp);
     rayTracer.setDepth(depth);
+    rayTracer.setSeed((uint32_t)seed);
     rayTracer.LoadObj(input, "");  // the MTL is read from the OBJ's directory
     rayTracer.setHostLight(light);
     rayTracer.setCamera(&camera);

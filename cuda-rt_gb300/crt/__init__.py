@@ -55,7 +55,7 @@ class _Light(C.Structure):
 
 class _RenderParams(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("spp", C.c_int32), ("row_begin", C.c_int32),
-                ("row_end", C.c_int32)]
+                ("row_end", C.c_int32), ("seed", C.c_uint32)]
 
 
 class _RenderOut(C.Structure):
@@ -260,10 +260,10 @@ class Scene:
         return (ids, t, nrm) if normals and not any_hit else (ids, t)
 
     def render(self, camera, light, width, height, spp, rows=None, out=None, aux=False, rays=False, rgbf=False,
-               rgbd=False, stream=None):
+               rgbd=False, stream=None, seed=0):
         """RayTracer::run + pullRaytracedImage.  Returns a dict of NumPy
         arrays unless `out` (a dict of preallocated buffers) is given."""
-        cam, lt, p = render_args(camera, light, width, height, spp, rows)
+        cam, lt, p = render_args(camera, light, width, height, spp, rows, seed)
         if out is None:
             npx, ns = width * height, width * height * spp
             out = dict(rgb8=np.zeros((npx, 3), np.uint8))
@@ -427,12 +427,12 @@ def write_bmp(path, rgb8, width, height):
     _check(lib().crt_write_bmp(os.fsencode(path), width, height, a.ctypes.data))
 
 
-def render_args(camera, light, width, height, spp, rows=None):
+def render_args(camera, light, width, height, spp, rows=None, seed=0):
     cam = _Camera(camera.fov, camera.focal_point, camera.fstop, (C.c_double * 3)(*camera.eye))
     lt = _Light((C.c_double * 3)(*light.color), (C.c_double * 3)(*light.position), light.radius,
                 light.constant_term, light.linear_term, light.quadratic_term)
     r0, r1 = rows if rows is not None else (0, 0)
-    return cam, lt, _RenderParams(width, height, spp, r0, r1)
+    return cam, lt, _RenderParams(width, height, spp, r0, r1, seed)
 
 
 def morton(verts, vidx, scene_box, codes, stream=None):

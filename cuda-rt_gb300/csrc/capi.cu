@@ -472,6 +472,7 @@ static crt_status render_args(crt_scene* s, const crt_camera* cam, const crt_lig
   a.lradius = light->radius;
   a.latt[0] = light->constant_term, a.latt[1] = light->linear_term, a.latt[2] = light->quadratic_term;
   a.counter = s->counter;
+  a.seed_mix = p->seed * 0x9E3779B1u;
   if (a.aperture != 0.0) {
     const LensTables t = lens_tables(st);
     a.lens_cs = t.cs, a.lens_sqrt = t.sq;

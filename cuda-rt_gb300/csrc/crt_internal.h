@@ -109,6 +109,7 @@ struct RenderArgs {
   double* rgbd = nullptr;     // optional: mean colour in double
   double* depth = nullptr;    // optional: mean hit t (misses count 0)
   int* shadow_id = nullptr;   // optional: occluding triangle per sample, -1 if none
+  uint32_t seed_mix = 0;             // XORed into each pixel's hash input (0: parity)
   const double2* lens_cs = nullptr;  // optional lens tables (lens.cu)
   const double* lens_sqrt = nullptr;
   // adjoint (grad_rgb != NULL selects it)

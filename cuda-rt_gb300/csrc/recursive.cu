@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(128) k_pixels_rec(DScene S, RenderArgs A, cons
     const int py = A.row0 + (tile / tiles_x) * 4 + (lane >> 3);
     const bool valid = px < A.W && py < A.row1;
     const int idx = (A.H - py - 1) * A.W + px;
-    uint32_t st = wang_hash((uint32_t)(((py / 16) * gx + px / 16) * 256 + (py % 16) * 16 + (px % 16)));
+    uint32_t st = wang_hash((uint32_t)(((py / 16) * gx + px / 16) * 256 + (py % 16) * 16 + (px % 16)) ^ A.seed_mix);
     const double xx = (2 * ((px + 0.5) * A.invW) - 1) * A.angle * A.aspect;
     const double yy = (1 - 2 * ((py + 0.5) * A.invH)) * A.angle;
     D3 fdir = normalize_exact(d3(xx, yy, -1.0));

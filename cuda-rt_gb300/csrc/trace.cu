@@ -92,7 +92,7 @@ __device__ __forceinline__ void pixel(const DScene& S, const RenderArgs& A, int 
     // getGlobalIdx_2D_2D (inc/indexing.h:4-9) of the pixel's thread in the
     // reference launch, seeded by initPNRG (kernels/mrand.cu:38-41).
     const uint32_t gid = (uint32_t)(((py / 16) * gx + px / 16) * 256 + (py % 16) * 16 + (px % 16));
-    uint32_t wst = wang_hash(gid);  // stream position at the start of the wave
+    uint32_t wst = wang_hash(gid ^ A.seed_mix);  // stream position at the start of the wave
     const double xx = (2 * ((px + 0.5) * A.invW) - 1) * A.angle * A.aspect;
     const double yy = (1 - 2 * ((py + 0.5) * A.invH)) * A.angle;
     // the pinhole direction scaled to the focal plane: the same for every sample

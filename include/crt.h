@@ -91,6 +91,9 @@ typedef struct crt_render_params {
   int32_t width, height;
   int32_t spp;                 /* samples per pixel (the reference fixes 20: raytracer.cu:138) */
   int32_t row_begin, row_end;  /* rows [begin, end) counted from the top; 0,0 = all */
+  uint32_t seed;               /* 0: the reference's per-pixel mrand streams (parity mode); any other
+                                  value XORs seed * 0x9E3779B1 into each pixel's hash input
+                                  (initPNRG, kernels/mrand.cu:38-41): an independent render */
 } crt_render_params;
 
 /* Outputs of crt_render.  Pixel (px, py), py counted from the top, is stored

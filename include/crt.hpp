@@ -185,13 +185,16 @@ class RayTracer {
   void setUpDevice(void* stream = nullptr) { scene_.setUpDevice(stream); }
   void setSamples(int spp) { spp_ = spp; }
   void setDepth(int depth) { depth_ = depth; }
+  /* 0 (default): the reference's random streams; other values: an
+   * independent render (crt_render_params.seed). */
+  void setSeed(uint32_t seed) { seed_ = seed; }
   /* runRayTracerKernelRec over the image (kernels/raytracer.cu:55-92). */
   void run(void* stream = nullptr) {
     if (!scene_.device()) throw std::logic_error("RayTracer::run before setUpDevice");
     const Camera cam = scene_.getCamera() ? *scene_.getCamera() : Camera();
     const crt_camera c = cam.to_c();
     const crt_light l = light_.to_c();
-    crt_render_params p{w_, h_, spp_, 0, 0};
+    crt_render_params p{w_, h_, spp_, 0, 0, seed_};
     crt_render_out o{};
     o.rgb8 = image_.data();
     if (depth_ == 0) {
@@ -219,6 +222,7 @@ class RayTracer {
  private:
   int w_, h_, super_;
   int spp_ = 20, depth_ = 0;
+  uint32_t seed_ = 0;
   std::vector<uint8_t> image_;
   Scene scene_;
   Light_h light_;

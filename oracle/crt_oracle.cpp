@@ -659,11 +659,13 @@ int orc_trace(void* h, const double* rays, int n, int any, int* ids, double* t, 
 //   shadow_id[idx*spp+k]  the occluding triangle when shadow is 1, else -1 (optional)
 //   rays_out[(idx*spp+k)*6]  the primary ray (optional)
 // rays_in (optional) replaces the generated primary ray of every sample; the
-// random draws are still consumed as in the reference.
+// random draws are still consumed as in the reference.  seed: 0 for the
+// reference's streams; otherwise seed * 0x9E3779B1 is XORed into each pixel's
+// hash input (the library's independent-render mode).
 // Returns the number of stack overflows.
 int orc_render(void* h, const orc_camera* cam, const orc_light* light, int W, int H, int spp, int row0,
                int row1, uint8_t* rgb8, double* color, int* hit_id, double* hit_t, int* shadow,
-               const double* rays_in, double* rays_out, int nthreads, int* shadow_id) {
+               const double* rays_in, double* rays_out, int nthreads, int* shadow_id, uint32_t seed) {
   const Scene* s = (const Scene*)h;
   const int gx = (W + 15) / 16;  // gridDim.x of the 16x16 launch (raytracer.cu:56-58)
   int overflow = 0;
@@ -681,7 +683,7 @@ int orc_render(void* h, const orc_camera* cam, const orc_light* light, int W, in
       // getGlobalIdx_2D_2D (inc/indexing.h:4-9) for block (px/16, py/16),
       // thread (px%16, py%16); initPNRG seeds it with wangHash.
       uint32_t g = (uint32_t)(((py / 16) * gx + px / 16) * 256 + (py % 16) * 16 + (px % 16));
-      uint32_t st = wang_hash(g);
+      uint32_t st = wang_hash(g ^ (seed * 0x9E3779B1u));  // seed 0: the reference's stream
       double xx = (2 * ((px + 0.5) * invW) - 1) * angle * aspect;
       double yy = (1 - 2 * ((py + 0.5) * invH)) * angle;
       V3 acc = v3(0, 0, 0);
@@ -745,7 +747,7 @@ int orc_render(void* h, const orc_camera* cam, const orc_light* light, int W, in
 // counts[2] (optional): closest-hit rays traced, shadow rays traced.
 int orc_render_rec(void* h, const orc_camera* cam, const orc_light* light, int W, int H, int spp, int depth,
                    const double* optics, uint8_t* rgb8, double* color, int* hit_id, double* hit_t,
-                   const double* rays_in, double* rays_out, int nthreads, int64_t* counts) {
+                   const double* rays_in, double* rays_out, int nthreads, int64_t* counts, uint32_t seed) {
   const Scene* s = (const Scene*)h;
   std::vector<double> opt(4 * (size_t)s->nmat);
   for (int m = 0; m < s->nmat; m++) {
@@ -766,7 +768,8 @@ int orc_render_rec(void* h, const orc_camera* cam, const orc_light* light, int W
   for (int py = 0; py < H; py++) {
     for (int px = 0; px < W; px++) {
       const int idx = (H - py - 1) * W + px;
-      uint32_t st = wang_hash((uint32_t)(((py / 16) * gx + px / 16) * 256 + (py % 16) * 16 + (px % 16)));
+      uint32_t st = wang_hash((uint32_t)(((py / 16) * gx + px / 16) * 256 + (py % 16) * 16 + (px % 16)) ^
+                              (seed * 0x9E3779B1u));
       double xx = (2 * ((px + 0.5) * invW) - 1) * angle * aspect;
       double yy = (1 - 2 * ((py + 0.5) * invH)) * angle;
       V3 acc = v3(0, 0, 0);

@@ -120,7 +120,7 @@ class OracleScene:
         return ids, t, nrm
 
     def render(self, cam, light, width, height, spp=None, rows=None, aux=False, rays_in=None, rays_out=False,
-               nthreads=0):
+               nthreads=0, seed=0):
         """Render rows [r0, r1) (default: all).  The reference ('ref') always
         takes 20 samples per pixel."""
         r0, r1 = rows if rows is not None else (0, height)
@@ -149,10 +149,10 @@ class OracleScene:
         f.restype = C.c_int
         f.argtypes = [C.c_void_p, C.POINTER(_Cam), C.POINTER(_Light), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
-                      C.c_void_p]
+                      C.c_void_p, C.c_uint32]
         g = lambda a: None if a is None else a.ctypes.data  # noqa: E731
         ov = f(self.h, C.byref(c), C.byref(L), width, height, spp, r0, r1, rgb.ctypes.data, col.ctypes.data,
-               g(hid), g(ht), g(sh), g(ri), g(ro), nthreads, g(shid))
+               g(hid), g(ht), g(sh), g(ri), g(ro), nthreads, g(shid), seed)
         out = dict(rgb=rgb, color=col, overflow=ov)
         if aux:
             out.update(hit_id=hid, hit_t=ht, shadow=sh, shadow_id=shid)
@@ -161,7 +161,8 @@ class OracleScene:
         return out
 
 
-def _render_rec(self, cam, light, width, height, spp, depth, optics=None, rays_in=None, rays_out=False, nthreads=0):
+def _render_rec(self, cam, light, width, height, spp, depth, optics=None, rays_in=None, rays_out=False, nthreads=0,
+                seed=0):
     """orc_render_rec: traceRay with `depth` levels of reflection and
     refraction.  optics: (num_materials, 4) kr xyz + ior, or None (kr = ks,
     ior = 1)."""
@@ -181,10 +182,11 @@ def _render_rec(self, cam, light, width, height, spp, depth, optics=None, rays_i
     f = self.lib.orc_render_rec
     f.restype = C.c_int
     f.argtypes = [C.c_void_p, C.POINTER(_Cam), C.POINTER(_Light), C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p,
-                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                  C.c_uint32]
     counts = np.zeros(2, np.int64)
     ov = f(self.h, C.byref(c), C.byref(L), width, height, spp, depth, g(op), rgb.ctypes.data, col.ctypes.data,
-           hid.ctypes.data, ht.ctypes.data, g(ri), g(ro), nthreads, counts.ctypes.data)
+           hid.ctypes.data, ht.ctypes.data, g(ri), g(ro), nthreads, counts.ctypes.data, seed)
     out = dict(rgb=rgb, color=col, hit_id=hid, hit_t=ht, overflow=ov, counts=counts.tolist())
     if rays_out:
         out["rays"] = ro

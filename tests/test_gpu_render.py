@@ -165,3 +165,24 @@ def test_lens_tables_give_identical_rays(cuda):
     for k in ("rays", "hit_id", "shadow", "rgb_f64", "rgb8"):
         assert_equal(on[k], off[k], k)
     assert np.abs(on["rays"][:, :2]).max() > 0.01  # the lens moved the origins
+
+
+def test_render_seed_mode(cuda):
+    """crt_render_params.seed: 0 is the reference's streams (parity mode);
+    another seed gives an independent render, the same on the GPU and in the
+    oracle (area light and thin lens, so every draw matters)."""
+    import crt
+    from crt import data
+    from oracle.oracle import OracleScene
+    sc = data.config1(nu=30, width=48, height=32, spp=4)
+    light = data.Light(position=sc.light.position, radius=0.4)
+    g, o = crt.Scene(sc.mesh), OracleScene(sc.mesh)
+    base = g.render(sc.camera, light, 48, 32, 4, aux=True, rays=True)
+    zero = g.render(sc.camera, light, 48, 32, 4, aux=True, rays=True, seed=0)
+    assert_equal(zero["rays"], base["rays"], "seed 0 is the default")
+    s7 = g.render(sc.camera, light, 48, 32, 4, aux=True, rays=True, rgbd=True, seed=7)
+    assert (s7["rays"] != base["rays"]).any()
+    ref = o.render(sc.camera, light, 48, 32, spp=4, aux=True, rays_in=s7["rays"], seed=7)
+    assert_equal(s7["hit_id"], ref["hit_id"], "hit ids, seed 7")
+    assert_equal(s7["shadow"], ref["shadow"], "shadow, seed 7")
+    assert_equal(s7["rgb8"], ref["rgb"], "rgb8, seed 7")
