@@ -99,6 +99,8 @@ def lib():
             "crt_render_recursive": [vp, vp, vp, vp, i32, vp, vp, vp],
             "crt_set_lens_tables": [i32],
             "crt_morton": [vp, vp, i32, vp, vp, vp],
+            "crt_hierarchy": [vp, vp, i32, vp, vp],
+            "crt_refit": [vp, i32, vp, i32, vp, vp, vp, vp],
             "crt_sort_pairs": [vp, vp, vp, vp, i32, i32, vp],
             "crt_sort_pairs_noalloc": [vp, vp, vp, vp, i32, i32, vp],
             "crt_scene_check": [vp, vp],

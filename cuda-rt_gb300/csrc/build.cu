@@ -1127,6 +1127,96 @@ cudaError_t launch_build_batch(const BatchBufs& b, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- stages
+// crt_hierarchy: the parent words of k_hierarchy turned into the reference's
+// HNode triplets (parent, left, right; a leaf holds its triangle id twice).
+__global__ void __launch_bounds__(256) k_nodes3(const uint32_t* __restrict__ parent,
+                                                const uint32_t* __restrict__ ids, int n,
+                                                int* __restrict__ nodes3) {
+  const int nn = 2 * n - 1;
+  for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < nn; x += gridDim.x * blockDim.x) {
+    if (x == 0) {
+      nodes3[0] = -1;  // the root
+    } else {
+      const uint32_t w = __ldg(parent + x);
+      const int p = (int)(w & kParentMask);
+      nodes3[3 * x] = p;
+      nodes3[3 * p + ((w & kParentLeft) ? 1 : 2)] = x;
+    }
+    if (x >= n - 1) {
+      const int id = (int)__ldg(ids + (x - (n - 1)));
+      nodes3[3 * x + 1] = id, nodes3[3 * x + 2] = id;
+    }
+  }
+}
+
+cudaError_t launch_stage_hierarchy(const uint32_t* codes, const uint32_t* ids, int n, int* nodes3,
+                                   uint32_t* parent, int* flags, WNode* wnodes, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  if (n >= 2) k_hierarchy<<<(n - 1 + 255) / 256, 256, 0, st>>>(codes, n, parent, flags, wnodes);
+  k_nodes3<<<(2 * n - 1 + 255) / 256, 256, 0, st>>>(parent, ids, n, nodes3);
+  return cudaGetLastError();
+}
+
+// crt_refit: RefitBounds (kernels/bvh.cu:209-258) on a caller's HNode
+// triplets: one climber per leaf, the second arrival at a node takes the
+// union of its children's boxes (bboxunion, bvh.cu:63-69) and climbs on.
+// Every index is range-checked (kErrIndex in *err) before it is followed.
+__global__ void __launch_bounds__(256) k_refit_nodes(const float* __restrict__ V, int nv,
+                                                     const int* __restrict__ vidx, int n,
+                                                     const uint32_t* __restrict__ ids,
+                                                     const int* __restrict__ nodes3, float* boxes, int* flags,
+                                                     int* err) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const int tri = (int)__ldg(ids + k);
+  if ((unsigned)tri >= (unsigned)n) {
+    atomicOr(err, kErrIndex);
+    return;
+  }
+  for (int j = 0; j < 3; j++)
+    if ((unsigned)__ldg(vidx + 3 * tri + j) >= (unsigned)nv) {
+      atomicOr(err, kErrIndex);
+      return;
+    }
+  float3 a, b, c;
+  float lo[3], hi[3];
+  tri_box(V, vidx, tri, a, b, c, lo, hi);
+  int x = (n - 1) + k;
+  for (int q = 0; q < 3; q++) __stcg(boxes + 6 * x + q, lo[q]), __stcg(boxes + 6 * x + 3 + q, hi[q]);
+  for (int level = 0; level < 2 * n; level++) {
+    const int p = __ldg(nodes3 + 3 * x);
+    if (p < 0) return;  // the root
+    if (p >= n - 1) {
+      atomicOr(err, kErrIndex);
+      return;
+    }
+    __threadfence();
+    if (atomicAdd(flags + p, 1) == 0) return;  // first arrival: the sibling climbs on
+    __threadfence();
+    const int l = __ldg(nodes3 + 3 * p + 1), r = __ldg(nodes3 + 3 * p + 2);
+    if ((unsigned)l >= (unsigned)(2 * n - 1) || (unsigned)r >= (unsigned)(2 * n - 1)) {
+      atomicOr(err, kErrIndex);
+      return;
+    }
+    const int o = (l == x) ? r : l;
+    for (int q = 0; q < 3; q++) {
+      lo[q] = fminf(lo[q], __ldcg(boxes + 6 * o + q));
+      hi[q] = fmaxf(hi[q], __ldcg(boxes + 6 * o + 3 + q));
+    }
+    x = p;
+    for (int q = 0; q < 3; q++) __stcg(boxes + 6 * x + q, lo[q]), __stcg(boxes + 6 * x + 3 + q, hi[q]);
+  }
+  atomicOr(err, kErrIndex);  // a cycle: only corrupt triplets get here
+}
+
+cudaError_t launch_stage_refit(const float* V, int nv, const int* vidx, int n, const uint32_t* ids,
+                               const int* nodes3, float* boxes, int* flags, int* err, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_refit_nodes<<<(n + 255) / 256, 256, 0, st>>>(V, nv, vidx, n, ids, nodes3, boxes, flags, err);
+  return cudaGetLastError();
+}
+
 // Index arrays that came from device memory (the host checks the others):
 // every vertex, normal and material index in range, or kErrIndex.  Reads
 // only the index arrays, so a bad index is reported before any kernel uses

@@ -630,6 +630,49 @@ crt_status crt_morton(const float* verts, const int32_t* vidx, int32_t n, const 
   return CRT_OK;
 }
 
+crt_status crt_hierarchy(const uint32_t* codes, const uint32_t* ids, int32_t n, int32_t* nodes3, void* stream) {
+  if (n < 0 || n > CRT_MAX_TRIANGLES || (n > 0 && (!codes || !ids || !nodes3))) return fail(CRT_INVALID_ARG, "bad arguments");
+  if (n == 0) return CRT_OK;
+  if (!(is_device_ptr(codes) && is_device_ptr(ids) && is_device_ptr(nodes3)))
+    return fail(CRT_INVALID_ARG, "crt_hierarchy takes device pointers");
+  cudaStream_t st = S(stream);
+  const size_t nn = 2 * (size_t)n - 1;
+  const size_t bytes = align256(4 * nn) + align256(4 * (size_t)n) + sizeof(WNode) * (size_t)n;
+  char* scratch = nullptr;
+  CRT_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scratch), bytes, st), "scratch");
+  uint32_t* parent = reinterpret_cast<uint32_t*>(scratch);
+  int* flags = reinterpret_cast<int*>(scratch + align256(4 * nn));
+  WNode* wnodes = reinterpret_cast<WNode*>(scratch + align256(4 * nn) + align256(4 * (size_t)n));
+  const cudaError_t e = launch_stage_hierarchy(codes, ids, n, nodes3, parent, flags, wnodes, st);
+  CRT_CUDA(cudaFreeAsync(scratch, st), "free");
+  CRT_CUDA(e, "hierarchy launch");
+  return CRT_OK;
+}
+
+crt_status crt_refit(const float* vertices, int32_t num_vertices, const int32_t* vertex_indices, int32_t n,
+                     const uint32_t* ids, const int32_t* nodes3, float* node_boxes, void* stream) {
+  if (n < 0 || n > CRT_MAX_TRIANGLES || num_vertices < 0 ||
+      (n > 0 && (!vertices || !vertex_indices || !ids || !nodes3 || !node_boxes)))
+    return fail(CRT_INVALID_ARG, "bad arguments");
+  if (n == 0) return CRT_OK;
+  if (!(is_device_ptr(vertices) && is_device_ptr(vertex_indices) && is_device_ptr(ids) && is_device_ptr(nodes3) &&
+        is_device_ptr(node_boxes)))
+    return fail(CRT_INVALID_ARG, "crt_refit takes device pointers");
+  cudaStream_t st = S(stream);
+  int* scratch = nullptr;  // [0] error bits, [1..n-1] arrival flags
+  CRT_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scratch), 4 * (size_t)n, st), "scratch");
+  CRT_CUDA(cudaMemsetAsync(scratch, 0, 4 * (size_t)n, st), "memset");
+  const cudaError_t e = launch_stage_refit(vertices, num_vertices, vertex_indices, n, ids, nodes3, node_boxes,
+                                           scratch + 1, scratch, st);
+  int err = 0;
+  if (e == cudaSuccess) CRT_CUDA(cudaMemcpyAsync(&err, scratch, sizeof(int), cudaMemcpyDeviceToHost, st), "read");
+  CRT_CUDA(cudaFreeAsync(scratch, st), "free");
+  CRT_CUDA(e, "refit launch");
+  CRT_CUDA(cudaStreamSynchronize(st), "synchronize");
+  if (err) return fail(CRT_INVALID_ARG, "an id, vertex index or node index is out of range");
+  return CRT_OK;
+}
+
 crt_status crt_sort_pairs(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, int32_t n,
                           int32_t key_bits, void* stream) {
   if (n < 0 || n > CRT_MAX_TRIANGLES || key_bits < 1 || key_bits > 32) return fail(CRT_INVALID_ARG, "bad sizes");

@@ -69,6 +69,12 @@ cudaError_t launch_build_batch(const BatchBufs& b, cudaStream_t st);
 // build.cu
 cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st);
 cudaError_t launch_refit(const MeshBufs& m, const BuildBufs& b, cudaStream_t st);
+// Stage-level hierarchy and refit in the reference's HNode layout (scratch:
+// parent 2n - 1 words, flags n - 1, wnodes n; flags zeroed by the caller).
+cudaError_t launch_stage_hierarchy(const uint32_t* codes, const uint32_t* ids, int n, int* nodes3,
+                                   uint32_t* parent, int* flags, WNode* wnodes, cudaStream_t st);
+cudaError_t launch_stage_refit(const float* V, int nv, const int* vidx, int n, const uint32_t* ids,
+                               const int* nodes3, float* boxes, int* flags, int* err, cudaStream_t st);
 // Range checks of device-resident index arrays (kErrIndex in b.g->err).
 cudaError_t launch_check_indices(const MeshBufs& m, const BuildBufs& b, cudaStream_t st);
 cudaError_t launch_morton(const float* verts, const int* vidx, int n, const float* box6, uint32_t* codes,

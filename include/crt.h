@@ -231,6 +231,19 @@ crt_status crt_adjoint_lambert(crt_scene* scene, const crt_camera* camera, const
  * kernels/bvh.cu:37-61), normalised by scene_box (6 floats, device). */
 crt_status crt_morton(const float* vertices, const int32_t* vertex_indices, int32_t num_triangles,
                       const float* scene_box, int32_t* codes, void* stream);
+/* Karras hierarchy (FindSpan / FindSplit / BuildHierarchy, kernels/bvh.cu:
+ * 100-207) of n sorted codes, with `ids` the sorted triangle ids: nodes3
+ * receives the (2n-1) HNode triplets (parent, left, right) in the reference's
+ * numbering (internal 0..n-2, root 0 with parent -1; leaf n-1+k holds ids[k]
+ * as left and right), as crt_bvh_export writes them.  Device pointers. */
+crt_status crt_hierarchy(const uint32_t* codes, const uint32_t* ids, int32_t n, int32_t* nodes3, void* stream);
+/* RefitBounds (kernels/bvh.cu:209-258) on given triplets: node_boxes
+ * [(2n-1)*6] receives every node's box (leaf n-1+k: the box of triangle
+ * ids[k]; internal: the union of its children), as crt_bvh_export writes
+ * sortedBBoxs.  Every id and index is range-checked on the device
+ * (CRT_INVALID_ARG).  Device pointers; synchronises `stream`. */
+crt_status crt_refit(const float* vertices, int32_t num_vertices, const int32_t* vertex_indices, int32_t n,
+                     const uint32_t* ids, const int32_t* nodes3, float* node_boxes, void* stream);
 /* Stable ascending LSD radix sort of (key, value) pairs on the low
  * `key_bits` bits of the keys (thrust::sort_by_key, kernels/bvh.cu:267-273).
  * vals_in may be NULL: values are then 0..n-1.  In and out arrays must not

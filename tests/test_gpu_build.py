@@ -108,3 +108,38 @@ def test_morton_stage_matches_oracle(cuda):
     crt.morton(v, vi, box, codes)
     torch.cuda.synchronize()
     assert_equal(codes.cpu().numpy(), ex["codes_unsorted"], "codes")
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 1000, 2049, 20000])
+def test_stage_hierarchy_and_refit(cuda, n):
+    """crt_hierarchy and crt_refit, the stage-level entry points, on the
+    sorted codes and ids of a build: the same HNode triplets and node boxes
+    as the full build's export (itself bit-exact against the oracle)."""
+    import torch
+    import crt
+    from crt import data
+    mesh = data.soup(n, seed=11 + n)
+    ex = crt.Scene(mesh).export()
+    dev = lambda a, dt: torch.as_tensor(np.ascontiguousarray(a).view(dt), device="cuda")  # noqa: E731
+    codes, ids = dev(ex["codes"], np.int32), dev(ex["ids"], np.int32)
+    nn = 2 * n - 1
+    nodes3 = torch.full((nn * 3,), -7, dtype=torch.int32, device="cuda")
+    lib = crt.lib()
+    assert lib.crt_hierarchy(codes.data_ptr(), ids.data_ptr(), n, nodes3.data_ptr(), None) == 0
+    assert_equal(nodes3.cpu().numpy().reshape(nn, 3), ex["nodes"], "nodes")
+    verts = dev(mesh.verts.astype(np.float32), np.float32)
+    vidx = dev(mesh.vidx.astype(np.int32), np.int32)
+    boxes = torch.full((nn * 6,), float("nan"), dtype=torch.float32, device="cuda")
+    assert lib.crt_refit(verts.data_ptr(), len(mesh.verts), vidx.data_ptr(), n, ids.data_ptr(), nodes3.data_ptr(),
+                         boxes.data_ptr(), None) == 0
+    assert_equal(boxes.cpu().numpy().reshape(nn, 6), ex["node_boxes"], "node boxes")
+    if n >= 2:  # corrupt triplets and ids are reported, not followed
+        bad = nodes3.clone()
+        bad[3 * (n - 1)] = 10 ** 6
+        assert lib.crt_refit(verts.data_ptr(), len(mesh.verts), vidx.data_ptr(), n, ids.data_ptr(), bad.data_ptr(),
+                             boxes.data_ptr(), None) == 1
+        bad_ids = ids.clone()
+        bad_ids[0] = n + 5
+        assert lib.crt_refit(verts.data_ptr(), len(mesh.verts), vidx.data_ptr(), n, bad_ids.data_ptr(),
+                             nodes3.data_ptr(), boxes.data_ptr(), None) == 1
+        assert "out of range" in lib.crt_last_error_string().decode()
