@@ -293,6 +293,7 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 }
 
 // Exclusive scan over the block of one value per thread; returns the prefix.
+template <int TH>
 __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_warp, uint32_t& total) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t x = v;
@@ -304,7 +305,7 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_warp
   if (lane == 31) s_warp[warp] = x;
   __syncthreads();
   uint32_t wpre = 0, tot = 0;
-  for (int w = 0; w < kSortThreads / 32; w++) {
+  for (int w = 0; w < TH / 32; w++) {
     const uint32_t s = s_warp[w];
     if (w < warp) wpre += s;
     tot += s;
@@ -317,42 +318,49 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_warp
 constexpr uint32_t kFlagAgg = 1u << 30, kFlagInc = 2u << 30, kValMask = (1u << 30) - 1;
 
 // One stable LSD pass over the digit at `shift` (thrust::sort_by_key's
-// role, kernels/bvh.cu:267-273).  Tiles of 2048 keys are claimed in order
-// from an atomic counter; within a tile, warps rank their 256 keys in input
-// order with __match_any_sync, and the tile's digit offsets come from a
-// decoupled look-back over the tiles before it.
-__global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __restrict__ kin,
+// role, kernels/bvh.cu:267-273).  Tiles of TH * IT keys are claimed in order
+// from an atomic counter; within a tile, warps rank their 32 * IT keys in
+// input order with __match_any_sync, and the tile's digit offsets come from a
+// decoupled look-back over the tiles before it.  Two shapes (sort_large):
+// 2048-key tiles of 256 threads for small inputs, 8192-key tiles of 1024
+// threads from 2^19 keys on (a quarter of the tiles, so a quarter of the
+// look-back chain; 45 us less per 1M-key build, 20 us more at 100k).
+template <int TH, int IT>
+__global__ void __launch_bounds__(TH) k_onesweep(const uint32_t* __restrict__ kin,
                                                            const uint32_t* __restrict__ vin,
                                                            uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
                                                            int n, int shift, const uint32_t* __restrict__ ghist,
                                                            uint32_t* __restrict__ status, unsigned* tile_counter,
                                                            int* err) {
-  constexpr int W = kSortThreads / 32;
+  constexpr int W = TH / 32;
+  constexpr int TILE = TH * IT;
+  constexpr int DPT = kRadix / TH;  // digits per thread
+  static_assert(kRadix % TH == 0 && 32 * IT < 65536, "digits per thread, 16-bit warp counters");
   __shared__ uint32_t s_whist[W][kRadix / 2];  // per-warp 16-bit digit counters
   __shared__ uint32_t s_tstart[kRadix];
   __shared__ uint32_t s_gbase[kRadix];
-  __shared__ uint32_t s_keys[kSortTile];
-  __shared__ uint32_t s_vals[kSortTile];
+  __shared__ uint32_t s_keys[TILE];
+  __shared__ uint32_t s_vals[TILE];
   __shared__ uint32_t s_warp[W];
   __shared__ int s_tile;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) s_tile = (int)atomicAdd(tile_counter, 1u);
-  for (int i = tid; i < W * kRadix / 2; i += kSortThreads) (&s_whist[0][0])[i] = 0;
+  for (int i = tid; i < W * kRadix / 2; i += TH) (&s_whist[0][0])[i] = 0;
   // global start of each digit: exclusive scan of the pass histogram
-  uint32_t gh[4], gsum = 0;
+  uint32_t gh[DPT], gsum = 0;
 #pragma unroll
-  for (int j = 0; j < 4; j++) gh[j] = __ldg(ghist + 4 * tid + j), gsum += gh[j];
+  for (int j = 0; j < DPT; j++) gh[j] = __ldg(ghist + DPT * tid + j), gsum += gh[j];
   uint32_t gtot;
-  uint32_t gpre = block_excl_scan(gsum, s_warp, gtot);
+  uint32_t gpre = block_excl_scan<TH>(gsum, s_warp, gtot);
   const int tile = s_tile;
-  const int base = tile * kSortTile;
+  const int base = tile * TILE;
   const uint32_t mask = kRadix - 1;
-  uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
+  uint32_t key[IT], val[IT], rank[IT];
   unsigned short* wh = reinterpret_cast<unsigned short*>(s_whist[warp]);
   const uint32_t lt = lanemask_lt();
 #pragma unroll
-  for (int r = 0; r < kSortItems; r++) {
-    const int idx = base + warp * (32 * kSortItems) + r * 32 + lane;
+  for (int r = 0; r < IT; r++) {
+    const int idx = base + warp * (32 * IT) + r * 32 + lane;
     const bool valid = idx < n;
     key[r] = valid ? __ldg(kin + idx) : 0u;
     val[r] = valid ? (vin ? __ldg(vin + idx) : (uint32_t)idx) : 0u;
@@ -370,10 +378,10 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
   }
   __syncthreads();
   // per digit: warp offsets (exclusive, in place) and the tile count
-  uint32_t cnt[4], csum = 0;
+  uint32_t cnt[DPT], csum = 0;
 #pragma unroll
-  for (int j = 0; j < 4; j++) {
-    const int d = 4 * tid + j;
+  for (int j = 0; j < DPT; j++) {
+    const int d = DPT * tid + j;
     uint32_t c = 0;
 #pragma unroll
     for (int w = 0; w < W; w++) {
@@ -388,22 +396,26 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
   // publish this tile's counts, then look back for the prefix over earlier tiles
   uint32_t* my = status + (size_t)tile * kRadix;
 #pragma unroll
-  for (int j = 0; j < 4; j++) st_relaxed(my + 4 * tid + j, (tile == 0 ? kFlagInc : kFlagAgg) | cnt[j]);
-  uint32_t pre[4] = {0, 0, 0, 0};
-  if (tile > 0) {
-    // The thread's four digits walk back together: four independent loads
-    // per L2 round trip.  A walk stops at the first inclusive prefix.
-    int look[4] = {tile - 1, tile - 1, tile - 1, tile - 1};
-    int spins = 0;
-    uint32_t live = 0xF;
-    while (live) {
-      uint32_t sv[4];
+  for (int j = 0; j < DPT; j++) st_relaxed(my + DPT * tid + j, (tile == 0 ? kFlagInc : kFlagAgg) | cnt[j]);
+  uint32_t pre[DPT];
 #pragma unroll
-      for (int j = 0; j < 4; j++)
-        sv[j] = (live >> j) & 1 ? ld_relaxed(status + (size_t)look[j] * kRadix + 4 * tid + j) : 0u;
+  for (int j = 0; j < DPT; j++) pre[j] = 0;
+  if (tile > 0) {
+    // The thread's DPT digits walk back together: DPT independent loads
+    // per L2 round trip.  A walk stops at the first inclusive prefix.
+    int look[DPT];
+#pragma unroll
+    for (int j = 0; j < DPT; j++) look[j] = tile - 1;
+    int spins = 0;
+    uint32_t live = (1u << DPT) - 1u;
+    while (live) {
+      uint32_t sv[DPT];
+#pragma unroll
+      for (int j = 0; j < DPT; j++)
+        sv[j] = (live >> j) & 1 ? ld_relaxed(status + (size_t)look[j] * kRadix + DPT * tid + j) : 0u;
       bool waiting = false;
 #pragma unroll
-      for (int j = 0; j < 4; j++) {
+      for (int j = 0; j < DPT; j++) {
         if (!((live >> j) & 1)) continue;
         const uint32_t f = sv[j] & ~kValMask;
         if (f == 0) {
@@ -413,7 +425,7 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
         pre[j] += sv[j] & kValMask;
         if (f == kFlagInc || look[j] == 0) {
           live &= ~(1u << j);
-          st_relaxed(my + 4 * tid + j, kFlagInc | (pre[j] + cnt[j]));
+          st_relaxed(my + DPT * tid + j, kFlagInc | (pre[j] + cnt[j]));
         } else {
           look[j]--;
         }
@@ -423,8 +435,8 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
         if (++spins > kSpinLimit || ((spins & 1023) == 0 && (ld_relaxed((const uint32_t*)err) & kErrTimeout))) {
           atomicOr(err, kErrTimeout);
 #pragma unroll
-          for (int j = 0; j < 4; j++)
-            if ((live >> j) & 1) st_relaxed(my + 4 * tid + j, kFlagInc | (pre[j] + cnt[j]));
+          for (int j = 0; j < DPT; j++)
+            if ((live >> j) & 1) st_relaxed(my + DPT * tid + j, kFlagInc | (pre[j] + cnt[j]));
           break;
         }
         __nanosleep(32);
@@ -432,12 +444,12 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
     }
   }
   uint32_t ctot;
-  uint32_t cpre = block_excl_scan(csum, s_warp, ctot);
+  uint32_t cpre = block_excl_scan<TH>(csum, s_warp, ctot);
   {
     uint32_t c = cpre, g = gpre;
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-      const int d = 4 * tid + j;
+    for (int j = 0; j < DPT; j++) {
+      const int d = DPT * tid + j;
       s_tstart[d] = c;
       s_gbase[d] = g + pre[j] - c;
       c += cnt[j];
@@ -446,8 +458,8 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
   }
   __syncthreads();
 #pragma unroll
-  for (int r = 0; r < kSortItems; r++) {
-    const int idx = base + warp * (32 * kSortItems) + r * 32 + lane;
+  for (int r = 0; r < IT; r++) {
+    const int idx = base + warp * (32 * IT) + r * 32 + lane;
     if (idx < n) {
       const uint32_t d = (key[r] >> shift) & mask;
       const uint32_t pos = s_tstart[d] + wh[d] + rank[r];
@@ -456,8 +468,8 @@ __global__ void __launch_bounds__(kSortThreads) k_onesweep(const uint32_t* __res
     }
   }
   __syncthreads();
-  const int tile_n = min(kSortTile, n - base);
-  for (int i = tid; i < tile_n; i += kSortThreads) {
+  const int tile_n = min(TILE, n - base);
+  for (int i = tid; i < tile_n; i += TH) {
     const uint32_t k = s_keys[i];
     const uint32_t pos = s_gbase[(k >> shift) & mask] + (uint32_t)i;
     kout[pos] = k;
@@ -1108,6 +1120,18 @@ int num_sms() {
   return sms;
 }
 
+// One sort pass in the shape sort_large(n) picks; `status` holds the
+// pass's sort_tiles(n) * kRadix words (enough for either shape).
+static void onesweep_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, int n, int shift,
+                          const uint32_t* ghist, uint32_t* status, unsigned* counter, int* err, cudaStream_t st) {
+  if (sort_large(n))
+    k_onesweep<kSortThreadsL, kSortItems><<<sort_tiles_used(n), kSortThreadsL, 0, st>>>(kin, vin, kout, vout, n, shift,
+                                                                                        ghist, status, counter, err);
+  else
+    k_onesweep<kSortThreads, kSortItems><<<sort_tiles_used(n), kSortThreads, 0, st>>>(kin, vin, kout, vout, n, shift,
+                                                                                      ghist, status, counter, err);
+}
+
 cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st) {
   const int n = m.ntri;
   if (n <= 0) return cudaSuccess;
@@ -1125,9 +1149,8 @@ cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st)
   for (int p = 0; p < passes; p++) {
     uint32_t* ko = (p & 1) ? b.keys_a : b.keys_b;
     uint32_t* vo = (p & 1) ? b.vals_a : b.vals_b;
-    k_onesweep<<<tiles, kSortThreads, 0, st>>>(kin, vin, ko, vo, n, p * kRadixBits, b.hist + p * kRadix,
-                                                b.status + (size_t)p * tiles * kRadix, &b.g->tile_counter[p],
-                                                &b.g->err);
+    onesweep_pass(kin, vin, ko, vo, n, p * kRadixBits, b.hist + p * kRadix, b.status + (size_t)p * tiles * kRadix,
+                  &b.g->tile_counter[p], &b.g->err, st);
     kin = ko;
     vin = vo;
   }
@@ -1153,16 +1176,16 @@ cudaError_t launch_build_batch(const BatchBufs& b, cudaStream_t st) {
   for (int p = 0; p < 3; p++) {
     uint32_t* ko = (p & 1) ? b.keys_a : b.keys_b;
     uint32_t* vo = (p & 1) ? b.vals_a : b.vals_b;
-    k_onesweep<<<tiles, kSortThreads, 0, st>>>(kin, vin, ko, vo, N, p * kRadixBits, b.hist + p * kRadix,
-                                                b.status + (size_t)p * tiles * kRadix, b.counters + p, b.err);
+    onesweep_pass(kin, vin, ko, vo, N, p * kRadixBits, b.hist + p * kRadix, b.status + (size_t)p * tiles * kRadix,
+                  b.counters + p, b.err, st);
     kin = ko;
     vin = vo;
   }
   // stable pass on the mesh id: ids end up grouped by mesh, by code within
   const int ge = min((N + 255) / 256, sms * 8);
   k_mesh_keys<<<ge, 256, 0, st>>>(b.vals_b, b.mesh_of, N, b.keys_a);
-  k_onesweep<<<tiles, kSortThreads, 0, st>>>(b.keys_a, b.vals_b, b.keys_b, b.vals_a, N, 0, b.hist + 3 * kRadix,
-                                              b.status + (size_t)3 * tiles * kRadix, b.counters + 3, b.err);
+  onesweep_pass(b.keys_a, b.vals_b, b.keys_b, b.vals_a, N, 0, b.hist + 3 * kRadix,
+                b.status + (size_t)3 * tiles * kRadix, b.counters + 3, b.err, st);
   k_gather_codes<<<ge, 256, 0, st>>>(b.vals_a, b.codes0, N, b.keys_b);
   if (b.NI > 0)
     k_hierarchy_batch<<<(b.NI + 255) / 256, 256, 0, st>>>(b.keys_b, b.tri_off, M, b.NI, b.parent, b.flags,
@@ -1335,8 +1358,8 @@ cudaError_t launch_sort_pairs(const uint32_t* kin, const uint32_t* vin, uint32_t
     const bool to_out = ((passes - 1 - p) & 1) == 0;
     uint32_t* ko = to_out ? kout : tk;
     uint32_t* vo = to_out ? vout : tv;
-    k_onesweep<<<tiles, kSortThreads, 0, st>>>(ki, vi, ko, vo, n, p * kRadixBits, hist + p * kRadix,
-                                                status + (size_t)p * tiles * kRadix, counters + p, err);
+    onesweep_pass(ki, vi, ko, vo, n, p * kRadixBits, hist + p * kRadix, status + (size_t)p * tiles * kRadix,
+                  counters + p, err, st);
     ki = ko;
     vi = vo;
   }

@@ -16,7 +16,13 @@ constexpr int kRadixBits = 10;
 constexpr int kRadix = 1 << kRadixBits;
 
 inline int sort_passes(int key_bits) { return (key_bits + kRadixBits - 1) / kRadixBits; }
+// Tiles of the small shape: an upper bound on the tiles of a pass, for sizing.
 inline int sort_tiles(int n) { return (n + kSortTile - 1) / kSortTile; }
+// From 2^19 keys on, passes use 8192-key tiles of 1024 threads.
+constexpr int kSortThreadsL = 1024;
+constexpr int kSortTileL = kSortThreadsL * kSortItems;
+inline bool sort_large(int n) { return n >= (1 << 19); }
+inline int sort_tiles_used(int n) { return sort_large(n) ? (n + kSortTileL - 1) / kSortTileL : sort_tiles(n); }
 
 // Device arrays of one scene's BVH build (owned by the scene).
 struct BuildBufs {
