@@ -56,3 +56,19 @@ def test_reference_arm_idle_on_other_ranks():
     import bench
     args = argparse.Namespace(steps=2, warmup=1)
     assert bench.run_reference(args, None, 1, 2) is None
+
+
+def test_clock_summary_keeps_the_timed_region():
+    """bench.Clocks keeps the nvidia-smi samples read inside the timed region
+    (plus one interval after it) and reports throttle reasons from them."""
+    import bench
+    c = bench.Clocks(0)
+    row = lambda t, mhz, cap: [t, str(mhz), "2070", "900", "Not Active", "Not Active", "Not Active", cap]  # noqa: E731
+    c.samples = [row(0.9, 1500, "Not Active"), row(1.05, 2070, "Not Active"), row(1.2, 2070, "Active"),
+                 row(2.5, 1200, "Not Active")]
+    c.t0, c.t1 = 1.0, 1.18
+    s = c.summary()
+    assert s["samples"] == 2 and s["sm_mhz"] == 2070.0 and s["reasons"] == ["sw_power_cap"]
+    assert c.summary() == s  # no side effects
+    c.t0, c.t1 = 3.0, 3.1  # nothing inside: the last samples stand in
+    assert c.summary()["samples"] == 2
