@@ -42,12 +42,13 @@ sys.path.insert(0, ROOT)
 METRIC = "LBVH build Mtris/s; closest-hit Mrays/s; batched+adjoint vs plain, 1 GB300"
 W, H, SPP = 1920, 1080, 16
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one k_pixels
-# launch of this frame, from an ncu --set full capture of this command; the
+# launch of this frame, from an ncu --set full capture of this command (of the
+# instrumented launch, the same kernel with traversal counters); the
 # fetched bytes (the `achieved` numerator) are mostly served by L1 and L2.
 # Most of these bytes are the lens-table lookups (two random loads per
 # sample, each filling whole L2 lines) and the threads' local memory
-# (traversal stacks and register spills of 155,648 resident threads).
-RENDER_DRAM_BYTES = 10_521_362_688
+# (traversal stacks and register spills of 175,104 resident threads).
+RENDER_DRAM_BYTES = 12_587_523_328
 
 
 def peaks():

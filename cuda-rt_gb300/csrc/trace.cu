@@ -372,7 +372,7 @@ __device__ __forceinline__ void flush_stats(const RenderArgs& A, const TravStats
 // SHORT: traversal-stack entries kept in shared memory per thread.
 constexpr int kPixelsShort = 0;
 template <int MODE>
-__global__ void __launch_bounds__(128, 8) k_pixels(DScene S, RenderArgs A) {
+__global__ void __launch_bounds__(128, 9) k_pixels(DScene S, RenderArgs A) {
   extern __shared__ int2 s_ring[];
   int2* ring = kPixelsShort > 0 ? s_ring + threadIdx.x : nullptr;
   TravStats ts;
