@@ -98,7 +98,7 @@ def lib():
             "crt_render": [vp, vp, vp, vp, vp, vp],
             "crt_render_recursive": [vp, vp, vp, vp, i32, vp, vp, vp],
             "crt_set_lens_tables": [i32],
-            "crt_morton": [vp, vp, i32, vp, vp, vp],
+            "crt_morton": [vp, i32, vp, i32, vp, vp, vp],
             "crt_hierarchy": [vp, vp, i32, vp, vp],
             "crt_refit": [vp, i32, vp, i32, vp, vp, vp, vp],
             "crt_sort_pairs": [vp, vp, vp, vp, i32, i32, vp],
@@ -439,8 +439,8 @@ def render_args(camera, light, width, height, spp, rows=None, seed=0):
 
 def morton(verts, vidx, scene_box, codes, stream=None):
     """crt_morton on device tensors."""
-    _check(lib().crt_morton(_addr(verts), _addr(vidx), int(vidx.shape[0]), _addr(scene_box), _addr(codes),
-                            _stream(stream)))
+    _check(lib().crt_morton(_addr(verts), int(verts.shape[0]), _addr(vidx), int(vidx.shape[0]), _addr(scene_box),
+                            _addr(codes), _stream(stream)))
 
 
 def sort_pairs(keys_in, vals_in, keys_out, vals_out, key_bits=32, stream=None):

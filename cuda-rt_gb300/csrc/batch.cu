@@ -125,6 +125,15 @@ crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* v
       delete b;
       return fail(CRT_INVALID_ARG, "crt_batch_create takes host meshes");
     }
+    // sizes, one mesh and the running totals (the offsets below are int32)
+    if (d.num_vertices <= 0 || d.num_normals <= 0 || (int64_t)vert_off[m] + d.num_vertices > CRT_MAX_VERTICES ||
+        (int64_t)nrm_off[m] + d.num_normals > CRT_MAX_VERTICES ||
+        (int64_t)b->tri_off[m] + d.num_triangles > CRT_MAX_TRIANGLES ||
+        (int64_t)mat_off[m] + d.num_materials > INT32_MAX || (int64_t)w.width * w.height > ((int64_t)1 << 30) ||
+        (int64_t)b->px_off[m] + (int64_t)w.width * w.height > INT32_MAX || w.spp > CRT_MAX_SPP) {
+      delete b;
+      return fail(CRT_INVALID_ARG, "batch mesh " + std::to_string(m) + ": a size is out of range");
+    }
     for (int64_t i = 0; i < 3 * (int64_t)d.num_triangles; i++) {
       const int32_t* ni = d.normal_indices ? d.normal_indices : d.vertex_indices;
       if (d.vertex_indices[i] < 0 || d.vertex_indices[i] >= d.num_vertices || ni[i] < 0 || ni[i] >= d.num_normals) {
@@ -150,10 +159,6 @@ crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* v
     b->views.push_back(w);
   }
   const int N = b->tri_off[M], V = vert_off[M], Nn = nrm_off[M], Mat = mat_off[M];
-  if ((int64_t)N > CRT_MAX_TRIANGLES) {
-    delete b;
-    return fail(CRT_INVALID_ARG, "too many triangles in the batch");
-  }
   b->N = N, b->V = V, b->Nn = Nn, b->Mat = Mat;
   // host staging of the concatenated arrays (indices made global)
   std::vector<float> hv(3 * (size_t)V), hn(3 * (size_t)Nn);

@@ -238,13 +238,21 @@ __global__ void __launch_bounds__(512, 2) k_morton(const float* __restrict__ V, 
     if (sh[i]) atomicAdd(&hist[i], sh[i]);
 }
 
-// Standalone Morton codes against a given scene box (crt_morton).
-__global__ void k_morton_only(const float* __restrict__ V, const int* __restrict__ vidx, int n,
-                              const float* __restrict__ box6, uint32_t* __restrict__ keys) {
+// Standalone Morton codes against a given scene box (crt_morton).  A
+// triangle with a vertex index outside [0, nv) sets *err and gets code 0; its
+// vertices are not read.
+__global__ void k_morton_only(const float* __restrict__ V, int nv, const int* __restrict__ vidx, int n,
+                              const float* __restrict__ box6, uint32_t* __restrict__ keys, int* err) {
   float mn[3], mx[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) mn[k] = box6[k], mx[k] = box6[3 + k];
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    if ((unsigned)__ldg(vidx + 3 * t) >= (unsigned)nv || (unsigned)__ldg(vidx + 3 * t + 1) >= (unsigned)nv ||
+        (unsigned)__ldg(vidx + 3 * t + 2) >= (unsigned)nv) {
+      atomicOr(err, 1);
+      keys[t] = 0u;
+      continue;
+    }
     float3 a, b, c;
     float lo[3], hi[3];
     tri_box(V, vidx, t, a, b, c, lo, hi);
@@ -1322,11 +1330,11 @@ cudaError_t launch_refit(const MeshBufs& m, const BuildBufs& b, cudaStream_t st)
   return cudaGetLastError();
 }
 
-cudaError_t launch_morton(const float* verts, const int* vidx, int n, const float* box6, uint32_t* codes,
-                          cudaStream_t st) {
+cudaError_t launch_morton(const float* verts, int nv, const int* vidx, int n, const float* box6, uint32_t* codes,
+                          int* err, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   const int g = min((n + 255) / 256, num_sms() * 8);
-  k_morton_only<<<g, 256, 0, st>>>(verts, vidx, n, box6, codes);
+  k_morton_only<<<g, 256, 0, st>>>(verts, nv, vidx, n, box6, codes, err);
   return cudaGetLastError();
 }
 

@@ -156,6 +156,8 @@ static crt_status create_scene(const crt_mesh_desc* d, void* stream, bool borrow
   const int n = d->num_triangles;
   if (n < 0 || n > CRT_MAX_TRIANGLES) return fail(CRT_INVALID_ARG, "num_triangles out of range");
   if (d->num_vertices < 0 || d->num_normals < 0) return fail(CRT_INVALID_ARG, "negative array size");
+  if (d->num_vertices > CRT_MAX_VERTICES || d->num_normals > CRT_MAX_VERTICES)
+    return fail(CRT_INVALID_ARG, "more than CRT_MAX_VERTICES vertices or normals");
   if (n > 0 && (!d->vertices || !d->vertex_indices || d->num_vertices <= 0))
     return fail(CRT_INVALID_ARG, "triangles need vertices and vertex_indices");
   if (n > 0 && (!d->normals || d->num_normals <= 0)) return fail(CRT_INVALID_ARG, "normals are required");
@@ -451,6 +453,7 @@ static crt_status render_args(crt_scene* s, const crt_camera* cam, const crt_lig
                               const crt_render_params* p, cudaStream_t st, RenderArgs& a) {
   if (!s->built) return fail(CRT_NOT_BUILT, "no BVH");
   if (p->width <= 0 || p->height <= 0 || p->spp <= 0) return fail(CRT_INVALID_ARG, "width, height, spp must be > 0");
+  if (p->spp > CRT_MAX_SPP) return fail(CRT_INVALID_ARG, "spp above CRT_MAX_SPP");
   if ((int64_t)p->width * p->height > (int64_t)1 << 30) return fail(CRT_INVALID_ARG, "image too large");
   int row0 = p->row_begin, row1 = p->row_end;
   if (row0 == 0 && row1 == 0) row1 = p->height;
@@ -621,12 +624,26 @@ crt_status crt_adjoint_lambert(crt_scene* s, const crt_camera* cam, const crt_li
   return check_globals(s, st);
 }
 
-crt_status crt_morton(const float* verts, const int32_t* vidx, int32_t n, const float* box6, int32_t* codes,
-                      void* stream) {
-  if (n < 0 || (n > 0 && (!verts || !vidx || !box6 || !codes))) return fail(CRT_INVALID_ARG, "bad arguments");
-  if (n > 0 && !(is_device_ptr(verts) && is_device_ptr(vidx) && is_device_ptr(box6) && is_device_ptr(codes)))
+crt_status crt_morton(const float* verts, int32_t num_vertices, const int32_t* vidx, int32_t n, const float* box6,
+                      int32_t* codes, void* stream) {
+  if (n < 0 || n > CRT_MAX_TRIANGLES || num_vertices < 0 || num_vertices > CRT_MAX_VERTICES ||
+      (n > 0 && (!verts || !vidx || !box6 || !codes)))
+    return fail(CRT_INVALID_ARG, "bad arguments");
+  if (n == 0) return CRT_OK;
+  if (!(is_device_ptr(verts) && is_device_ptr(vidx) && is_device_ptr(box6) && is_device_ptr(codes)))
     return fail(CRT_INVALID_ARG, "crt_morton takes device pointers");
-  CRT_CUDA(launch_morton(verts, vidx, n, box6, reinterpret_cast<uint32_t*>(codes), S(stream)), "morton launch");
+  cudaStream_t st = S(stream);
+  int* scratch = nullptr;  // error bit
+  CRT_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scratch), sizeof(int), st), "scratch");
+  CRT_CUDA(cudaMemsetAsync(scratch, 0, sizeof(int), st), "memset");
+  const cudaError_t e =
+      launch_morton(verts, num_vertices, vidx, n, box6, reinterpret_cast<uint32_t*>(codes), scratch, st);
+  int err = 0;
+  if (e == cudaSuccess) CRT_CUDA(cudaMemcpyAsync(&err, scratch, sizeof(int), cudaMemcpyDeviceToHost, st), "read");
+  CRT_CUDA(cudaFreeAsync(scratch, st), "free");
+  CRT_CUDA(e, "morton launch");
+  CRT_CUDA(cudaStreamSynchronize(st), "synchronize");
+  if (err) return fail(CRT_INVALID_ARG, "a vertex index is out of range");
   return CRT_OK;
 }
 
@@ -651,7 +668,7 @@ crt_status crt_hierarchy(const uint32_t* codes, const uint32_t* ids, int32_t n, 
 
 crt_status crt_refit(const float* vertices, int32_t num_vertices, const int32_t* vertex_indices, int32_t n,
                      const uint32_t* ids, const int32_t* nodes3, float* node_boxes, void* stream) {
-  if (n < 0 || n > CRT_MAX_TRIANGLES || num_vertices < 0 ||
+  if (n < 0 || n > CRT_MAX_TRIANGLES || num_vertices < 0 || num_vertices > CRT_MAX_VERTICES ||
       (n > 0 && (!vertices || !vertex_indices || !ids || !nodes3 || !node_boxes)))
     return fail(CRT_INVALID_ARG, "bad arguments");
   if (n == 0) return CRT_OK;

@@ -83,8 +83,8 @@ cudaError_t launch_stage_refit(const float* V, int nv, const int* vidx, int n, c
                                const int* nodes3, float* boxes, int* flags, int* err, cudaStream_t st);
 // Range checks of device-resident index arrays (kErrIndex in b.g->err).
 cudaError_t launch_check_indices(const MeshBufs& m, const BuildBufs& b, cudaStream_t st);
-cudaError_t launch_morton(const float* verts, const int* vidx, int n, const float* box6, uint32_t* codes,
-                          cudaStream_t st);
+cudaError_t launch_morton(const float* verts, int nv, const int* vidx, int n, const float* box6, uint32_t* codes,
+                          int* err, cudaStream_t st);
 // Stable LSD radix sort; scratch holds sort_scratch_bytes(n, key_bits).
 size_t sort_scratch_bytes(int n, int key_bits);
 cudaError_t launch_sort_pairs(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, int n,

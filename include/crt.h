@@ -38,6 +38,12 @@ typedef enum crt_status {
  * below 62, so the reference's 64-entry traversal stack (kernels/bvh.cu:379)
  * can never overflow. */
 #define CRT_MAX_TRIANGLES (1 << 28)
+/* Largest vertex (and normal) count: three coordinates per vertex keep every
+ * float offset within int32. */
+#define CRT_MAX_VERTICES (1 << 29)
+/* Largest samples-per-pixel count of a render; an image holds at most 2^30
+ * pixels (width * height). */
+#define CRT_MAX_SPP (1 << 24)
 
 typedef struct crt_scene crt_scene;
 
@@ -55,9 +61,9 @@ typedef struct crt_material {
  * normal_indices may be NULL (then vertex_indices index the normals too);
  * material_ids may be NULL (every triangle uses material 0). */
 typedef struct crt_mesh_desc {
-  const float* vertices;   /* num_vertices * 3 */
+  const float* vertices;   /* num_vertices * 3; num_vertices <= CRT_MAX_VERTICES */
   int32_t num_vertices;
-  const float* normals;    /* num_normals * 3 */
+  const float* normals;    /* num_normals * 3; num_normals <= CRT_MAX_VERTICES */
   int32_t num_normals;
   const int32_t* vertex_indices; /* num_triangles * 3 */
   const int32_t* normal_indices; /* num_triangles * 3 or NULL */
@@ -89,7 +95,7 @@ typedef struct crt_light {
 
 typedef struct crt_render_params {
   int32_t width, height;
-  int32_t spp;                 /* samples per pixel (the reference fixes 20: raytracer.cu:138) */
+  int32_t spp;                 /* samples per pixel, 1..CRT_MAX_SPP (the reference fixes 20: raytracer.cu:138) */
   int32_t row_begin, row_end;  /* rows [begin, end) counted from the top; 0,0 = all */
   uint32_t seed;               /* 0: the reference's per-pixel mrand streams (parity mode); any other
                                   value XORs seed * 0x9E3779B1 into each pixel's hash input
@@ -199,11 +205,12 @@ crt_status crt_render_recursive(crt_scene* scene, const crt_camera* camera, cons
  * thin-lens sample needs cos/sin(2*pi*u1) and sqrt(u2) in double for two
  * mrand draws (raytracer.cu:141-142); a draw takes one of 83,886,081
  * values, so the library tabulates both functions at every value once per
- * device (2.0 GB of device memory, built in about 10 ms by the same double
+ * device (2.0 GB of device memory, built in about 6 ms by the same double
  * expressions) and the kernels load them instead of computing them.  Images
  * are identical either way.  On by default; built at the first thin-lens
  * render or batch creation on a device with 8 GB to spare, outside stream
- * capture.  enable = 0 turns them off for later calls (the memory stays). */
+ * capture, and held until the process exits.  enable = 0 turns them off for
+ * later calls (the memory stays allocated). */
 crt_status crt_set_lens_tables(int32_t enable);
 
 /* Replace the material table (same count as at creation), e.g. new
@@ -226,11 +233,14 @@ crt_status crt_adjoint_lambert(crt_scene* scene, const crt_camera* camera, const
                                const crt_render_params* params, const double* grad_rgb, const double* grad_depth,
                                double* grad_vertices, double* grad_light, double* grad_kd, void* stream);
 
-/* ---- stage-level entry points (device pointers only, asynchronous) ----
+/* ---- stage-level entry points (device pointers only) ----
  * Morton codes of each triangle's centroid (computeMortonCodesKernel,
- * kernels/bvh.cu:37-61), normalised by scene_box (6 floats, device). */
-crt_status crt_morton(const float* vertices, const int32_t* vertex_indices, int32_t num_triangles,
-                      const float* scene_box, int32_t* codes, void* stream);
+ * kernels/bvh.cu:37-61), normalised by scene_box (6 floats, device).  Every
+ * vertex index is range-checked on the device against num_vertices
+ * (CRT_INVALID_ARG; such a triangle's vertices are not read and its code is
+ * 0).  Synchronises `stream`. */
+crt_status crt_morton(const float* vertices, int32_t num_vertices, const int32_t* vertex_indices,
+                      int32_t num_triangles, const float* scene_box, int32_t* codes, void* stream);
 /* Karras hierarchy (FindSpan / FindSplit / BuildHierarchy, kernels/bvh.cu:
  * 100-207) of n sorted codes, with `ids` the sorted triangle ids: nodes3
  * receives the (2n-1) HNode triplets (parent, left, right) in the reference's

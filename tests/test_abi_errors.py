@@ -81,3 +81,55 @@ def test_loader_and_writer_refuse_bad_arguments(lib, tmp_path):
     assert lib.crt_obj_load(None, None, C.byref(h)) == INVALID
     assert lib.crt_write_bmp(str(tmp_path / "x.bmp").encode(), 0, 4, None) == INVALID
     assert lib.crt_obj_free(None) == 0
+
+
+def _big_desc(nv, nn, n=1):
+    """A description whose counts exceed a limit while its arrays are small:
+    the counts are refused before any array is read."""
+    import crt
+    keep = [np.zeros(9, np.float32), np.zeros(9, np.float32), np.zeros(3, np.int32), crt._Material()]
+    d = crt._MeshDesc(keep[0].ctypes.data, nv, keep[1].ctypes.data, nn, keep[2].ctypes.data, None, n,
+                      C.addressof(keep[3]), 1, None)
+    return d, keep
+
+
+def test_vertex_and_normal_counts_are_bounded(lib):
+    """CRT_MAX_VERTICES keeps every 3 * index float offset within int32."""
+    out = C.c_void_p()
+    for nv, nn in (((1 << 29) + 1, 3), (3, (1 << 29) + 1)):
+        d, keep = _big_desc(nv, nn)
+        assert lib.crt_scene_create(C.byref(d), None, C.byref(out)) == INVALID
+        assert "CRT_MAX_VERTICES" in error(lib)
+        assert lib.crt_scene_create_borrowed(C.byref(d), None, C.byref(out)) == INVALID
+    assert not out.value
+    big = (1 << 29) + 1
+    assert lib.crt_refit(None, big, None, 4, None, None, None, None) == INVALID
+    assert lib.crt_morton(None, big, None, 4, None, None, None) == INVALID
+    assert lib.crt_morton(None, 3, None, (1 << 28) + 1, None, None, None) == INVALID
+    assert lib.crt_morton(None, 3, None, 0, None, None, None) == 0  # nothing to do
+
+
+def test_batch_create_refuses_oversized_meshes_and_views(lib):
+    """Per-mesh counts, running totals and view sizes are checked in 64-bit
+    before the int32 offsets of the concatenated arrays are formed."""
+    import crt
+    out = C.c_void_p()
+
+    def attempt(d, width=8, height=8, spp=1, m=1):
+        views = (crt._BatchView * m)()
+        for v in views:
+            v.width, v.height, v.spp = width, height, spp
+        descs = (crt._MeshDesc * m)(*([d] * m))
+        return lib.crt_batch_create(descs, views, m, None, C.byref(out))
+
+    d, keep = _big_desc((1 << 29) + 1, 3)
+    assert attempt(d) == INVALID and "size is out of range" in error(lib)
+    d, keep = _big_desc(3, 3)
+    assert attempt(d, width=1 << 16, height=1 << 15) == INVALID and "size is out of range" in error(lib)
+    assert attempt(d, spp=(1 << 24) + 1) == INVALID and "size is out of range" in error(lib)
+    # each view fits, the total pixel count does not
+    assert attempt(d, width=1 << 15, height=1 << 15, m=2) == INVALID and "batch mesh 1" in error(lib)
+    # each mesh fits, the total vertex count does not
+    d, keep = _big_desc(1 << 28, 3)
+    assert attempt(d, m=3) == INVALID and "batch mesh 2" in error(lib)
+    assert not out.value

@@ -108,6 +108,17 @@ def test_morton_stage_matches_oracle(cuda):
     crt.morton(v, vi, box, codes)
     torch.cuda.synchronize()
     assert_equal(codes.cpu().numpy(), ex["codes_unsorted"], "codes")
+    # an index one past the last vertex, and a negative one: refused, and
+    # only those triangles lose their codes (their vertices are not read)
+    bad = m.vidx.copy()
+    bad[17, 1] = m.verts.shape[0]
+    bad[4000, 2] = -1
+    codes.fill_(-1)
+    with pytest.raises(crt.CrtError, match="vertex index"):
+        crt.morton(v, torch.from_numpy(bad).cuda(), box, codes)
+    want = ex["codes_unsorted"].copy()
+    want[[17, 4000]] = 0
+    assert_equal(codes.cpu().numpy(), want, "codes beside the bad triangles")
 
 
 @pytest.mark.parametrize("n", [1, 2, 3, 1000, 2049, 20000])
