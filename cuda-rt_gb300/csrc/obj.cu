@@ -13,16 +13,27 @@
 // is skipped, as tinyobjloader warns and goes on; a mesh without materials
 // gets one Lambert material (kd 0.8).  Every face corner must name a normal:
 // the reference reads normals[-1] otherwise, so such files are rejected.
+//
+// The OBJ is read in chunks of whole lines on all host cores, in two passes:
+// the first counts each chunk's lines, vertices, normals and triangles and
+// lists its mtllib/usemtl lines; a serial step reads the MTL files and
+// resolves every usemtl in file order and gives each chunk its starting
+// offsets; the second parses each chunk into its place in the output arrays
+// (a relative index counts back from the vertices before its line, as in a
+// serial read).  The result does not depend on the chunking; the first error
+// in file order is the one reported.
+#include <algorithm>
+#include <atomic>
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
-#include <iterator>
 #include <map>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "crt.h"
@@ -143,18 +154,168 @@ bool tok_corner(const Tok& t, size_t nv, size_t nn, int& vi, int& ni) {
   if (ve == t.b) return false;
   char* e = nullptr;
   const long v = std::strtol(t.b, &e, 10);
-  if (e != ve || v == 0) return false;
+  if (e != ve || v == 0 || v > INT32_MAX || v < -(long)INT32_MAX) return false;
   vi = v > 0 ? (int)(v - 1) : (int)((long)nv + v);
   ni = -1;
   if (s1) {
     const char* s2 = static_cast<const char*>(std::memchr(s1 + 1, '/', t.e - (s1 + 1)));
     if (s2 && s2 + 1 < t.e) {
       const long n = std::strtol(s2 + 1, &e, 10);
-      if (e != t.e || n == 0) return false;
+      if (e != t.e || n == 0 || n > INT32_MAX || n < -(long)INT32_MAX) return false;
       ni = n > 0 ? (int)(n - 1) : (int)((long)nn + n);
     }
   }
   return true;
+}
+
+// Whole file into buf (NUL-terminated, so strtod never reads past it).
+bool read_file(const char* path, std::string& buf) {
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return false;
+  bool ok = std::fseek(f, 0, SEEK_END) == 0;
+  const long size = ok ? std::ftell(f) : -1;
+  ok = ok && size >= 0 && std::fseek(f, 0, SEEK_SET) == 0;
+  if (ok) {
+    buf.resize((size_t)size);
+    ok = size == 0 || std::fread(&buf[0], 1, (size_t)size, f) == (size_t)size;
+  }
+  std::fclose(f);
+  return ok;
+}
+
+// Whitespace-separated tokens of the line [q, le).
+void tokenize(const char* q, const char* le, std::vector<Tok>& t) {
+  t.clear();
+  while (q < le) {
+    while (q < le && space(*q)) q++;
+    const char* tb = q;
+    while (q < le && !space(*q)) q++;
+    if (q > tb) t.push_back(Tok{tb, q});
+  }
+}
+
+// A run of whole lines [b, e), its counts (first pass), its offsets in the
+// file and the output arrays (serial step) and its first error (second pass).
+struct Chunk {
+  struct Event {  // an mtllib or usemtl line
+    bool lib, has_name;
+    std::string name;
+  };
+  const char* b;
+  const char* e;
+  int64_t lines = 0, nv = 0, nn = 0, ntri = 0;
+  std::vector<Event> events;
+  int64_t line0 = 0, v0 = 0, n0 = 0, t0 = 0;
+  int mat0 = -1;
+  std::vector<int> usemtl;  // the material each of its usemtl lines selects
+  std::string err;
+};
+
+// Chunks of about CRT_OBJ_CHUNK_BYTES (environment; default 256 KiB), each
+// ending just after a newline (the last at the end of the file).
+std::vector<Chunk> split_chunks(const std::string& buf) {
+  size_t want = (size_t)1 << 18;
+  if (const char* ev = std::getenv("CRT_OBJ_CHUNK_BYTES")) {
+    const long x = std::strtol(ev, nullptr, 10);
+    if (x > 0) want = (size_t)x;
+  }
+  std::vector<Chunk> out;
+  const char* p = buf.c_str();
+  const char* const end = p + buf.size();
+  while (p < end) {
+    const char* q = (size_t)(end - p) > want ? p + want : end;
+    if (q < end) {
+      const char* nl = static_cast<const char*>(std::memchr(q - 1, '\n', end - (q - 1)));
+      q = nl ? nl + 1 : end;
+    }
+    Chunk c;
+    c.b = p, c.e = q;
+    out.push_back(std::move(c));
+    p = q;
+  }
+  return out;
+}
+
+// f(i) for i in [0, n) on nth threads (this one included).
+template <typename F>
+void parallel_for(size_t n, size_t nth, F f) {
+  std::atomic<size_t> next(0);
+  auto work = [&]() {
+    for (size_t i; (i = next.fetch_add(1)) < n;) f(i);
+  };
+  std::vector<std::thread> pool;
+  for (size_t k = 1; k < nth; k++) pool.emplace_back(work);
+  work();
+  for (std::thread& th : pool) th.join();
+}
+
+// First pass: counts and mtllib/usemtl lines.
+void count_chunk(Chunk& c) {
+  std::vector<Tok> t;
+  for (const char* p = c.b; p < c.e;) {
+    const char* le = static_cast<const char*>(std::memchr(p, '\n', c.e - p));
+    if (!le) le = c.e;
+    c.lines++;
+    tokenize(p, le, t);
+    p = le + 1;
+    if (t.empty() || *t[0].b == '#') continue;
+    if (t[0].is("v")) c.nv++;
+    else if (t[0].is("vn")) c.nn++;
+    else if (t[0].is("f")) c.ntri += t.size() >= 4 ? (int64_t)t.size() - 3 : 0;
+    else if (t[0].is("mtllib") && t.size() >= 2) c.events.push_back(Chunk::Event{true, true, t[1].str()});
+    else if (t[0].is("usemtl")) c.events.push_back(Chunk::Event{false, t.size() >= 2, t.size() >= 2 ? t[1].str() : ""});
+  }
+}
+
+// Second pass: the chunk's vertices, normals and triangles into their places.
+void parse_chunk(Chunk& c, crt_obj& o) {
+  std::vector<Tok> t;
+  std::vector<int> cv, cn;
+  int64_t line = c.line0, lv = c.v0, ln = c.n0, lt = c.t0;
+  int cur = c.mat0;
+  size_t ue = 0;
+  for (const char* p = c.b; p < c.e;) {
+    const char* le = static_cast<const char*>(std::memchr(p, '\n', c.e - p));
+    if (!le) le = c.e;
+    line++;
+    tokenize(p, le, t);
+    p = le + 1;
+    if (t.empty() || *t[0].b == '#') continue;
+    if (t[0].is("v") || t[0].is("vn")) {
+      double x[3];
+      bool ok = t.size() >= 4;
+      for (int k = 0; ok && k < 3; k++) ok = tok_double(t[1 + k], x[k]);
+      if (!ok) {
+        c.err = "bad vertex at line " + std::to_string(line);
+        return;
+      }
+      float* dst = t[0].is("v") ? &o.v[3 * (size_t)lv++] : &o.n[3 * (size_t)ln++];
+      for (int k = 0; k < 3; k++) dst[k] = (float)x[k];
+    } else if (t[0].is("usemtl")) {
+      cur = c.usemtl[ue++];
+    } else if (t[0].is("f")) {
+      cv.clear();
+      cn.clear();
+      for (size_t k = 1; k < t.size(); k++) {
+        int vi, ni;
+        if (!tok_corner(t[k], (size_t)lv, (size_t)ln, vi, ni)) {
+          c.err = "bad face corner at line " + std::to_string(line);
+          return;
+        }
+        if (ni < 0) {
+          c.err = "face without a normal index at line " + std::to_string(line) + " (vn normals are required)";
+          return;
+        }
+        cv.push_back(vi);
+        cn.push_back(ni);
+      }
+      for (size_t k = 1; k + 1 < cv.size(); k++, lt++) {
+        const size_t c3[3] = {0, k, k + 1};
+        for (int j = 0; j < 3; j++) o.vi[3 * (size_t)lt + j] = cv[c3[j]], o.ni[3 * (size_t)lt + j] = cn[c3[j]];
+        o.mid[(size_t)lt] = cur;
+      }
+    }
+  }
 }
 
 }  // namespace
@@ -164,72 +325,49 @@ extern "C" {
 crt_status crt_obj_load(const char* obj_path, const char* mtl_dir, crt_obj** out) {
   if (!obj_path || !out) return fail("null argument");
   *out = nullptr;
-  std::ifstream f(obj_path, std::ios::binary);
-  if (!f) return fail(std::string("cannot open ") + obj_path);
-  std::string buf((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+  std::string buf;
+  if (!read_file(obj_path, buf)) return fail(std::string("cannot open ") + obj_path);
   const std::string base = mtl_dir ? std::string(mtl_dir) : dir_of(obj_path);
+  std::vector<Chunk> chunks = split_chunks(buf);
+  const size_t nth = std::min<size_t>(chunks.size(), std::max(1u, std::thread::hardware_concurrency()));
+  parallel_for(chunks.size(), nth, [&](size_t c) { count_chunk(chunks[c]); });
+
+  // serial: MTL files and usemtl in file order, each chunk's offsets
   crt_obj* o = new crt_obj;
   std::map<std::string, int> names;
   int cur = -1;
-  size_t lineno = 0;
-  std::vector<Tok> t;
-  std::vector<int> cv, cn;
-  const char* p = buf.c_str();
-  const char* const end = p + buf.size();
-  while (p < end) {
-    const char* le = static_cast<const char*>(std::memchr(p, '\n', end - p));
-    if (!le) le = end;
-    lineno++;
-    t.clear();
-    for (const char* q = p; q < le;) {
-      while (q < le && space(*q)) q++;
-      const char* tb = q;
-      while (q < le && !space(*q)) q++;
-      if (q > tb) t.push_back(Tok{tb, q});
-    }
-    p = le + 1;
-    if (t.empty() || *t[0].b == '#') continue;
-    if (t[0].is("v") || t[0].is("vn")) {
-      double x[3];
-      bool ok = t.size() >= 4;
-      for (int k = 0; ok && k < 3; k++) ok = tok_double(t[1 + k], x[k]);
-      if (!ok) {
-        delete o;
-        return fail("bad vertex at line " + std::to_string(lineno));
-      }
-      std::vector<float>& dst = t[0].is("v") ? o->v : o->n;
-      for (int k = 0; k < 3; k++) dst.push_back((float)x[k]);
-    } else if (t[0].is("mtllib") && t.size() >= 2) {
-      std::string mp = base;
-      if (!mp.empty() && mp.back() != '/') mp += '/';
-      read_mtl(mp + t[1].str(), names, o->mats, o->ior);
-    } else if (t[0].is("usemtl")) {
-      const auto it = t.size() >= 2 ? names.find(t[1].str()) : names.end();
-      cur = it == names.end() ? -1 : it->second;
-    } else if (t[0].is("f")) {
-      cv.clear();
-      cn.clear();
-      for (size_t k = 1; k < t.size(); k++) {
-        int vi, ni;
-        if (!tok_corner(t[k], o->v.size() / 3, o->n.size() / 3, vi, ni)) {
-          delete o;
-          return fail("bad face corner at line " + std::to_string(lineno));
-        }
-        if (ni < 0) {
-          delete o;
-          return fail("face without a normal index at line " + std::to_string(lineno) +
-                      " (vn normals are required)");
-        }
-        cv.push_back(vi);
-        cn.push_back(ni);
-      }
-      for (size_t k = 1; k + 1 < cv.size(); k++) {
-        const size_t c3[3] = {0, k, k + 1};
-        for (size_t j : c3) o->vi.push_back(cv[j]), o->ni.push_back(cn[j]);
-        o->mid.push_back(cur);
+  int64_t L = 0, V = 0, N = 0, T = 0;
+  for (Chunk& c : chunks) {
+    c.line0 = L, c.v0 = V, c.n0 = N, c.t0 = T, c.mat0 = cur;
+    for (const Chunk::Event& ev : c.events) {
+      if (ev.lib) {
+        std::string mp = base;
+        if (!mp.empty() && mp.back() != '/') mp += '/';
+        read_mtl(mp + ev.name, names, o->mats, o->ior);
+      } else {
+        const auto it = ev.has_name ? names.find(ev.name) : names.end();
+        cur = it == names.end() ? -1 : it->second;
+        c.usemtl.push_back(cur);
       }
     }
+    L += c.lines, V += c.nv, N += c.nn, T += c.ntri;
   }
+  if (V > CRT_MAX_VERTICES || N > CRT_MAX_VERTICES || T > CRT_MAX_TRIANGLES) {
+    delete o;
+    return fail("more than CRT_MAX_VERTICES vertices or normals, or CRT_MAX_TRIANGLES triangles");
+  }
+  o->v.resize(3 * (size_t)V);
+  o->n.resize(3 * (size_t)N);
+  o->vi.resize(3 * (size_t)T);
+  o->ni.resize(3 * (size_t)T);
+  o->mid.resize((size_t)T);
+  parallel_for(chunks.size(), nth, [&](size_t c) { parse_chunk(chunks[c], *o); });
+  for (const Chunk& c : chunks)
+    if (!c.err.empty()) {
+      delete o;
+      return fail(c.err);
+    }
+
   if (o->mats.empty()) {
     crt_material z;
     std::memset(&z, 0, sizeof(z));
@@ -239,9 +377,8 @@ crt_status crt_obj_load(const char* obj_path, const char* mtl_dir, crt_obj** out
   }
   for (int32_t& m : o->mid)
     if (m < 0) m = 0;
-  const int64_t nv = (int64_t)o->v.size() / 3, nn = (int64_t)o->n.size() / 3;
   for (size_t k = 0; k < o->vi.size(); k++)
-    if (o->vi[k] < 0 || o->vi[k] >= nv || o->ni[k] < 0 || o->ni[k] >= nn) {
+    if (o->vi[k] < 0 || o->vi[k] >= V || o->ni[k] < 0 || o->ni[k] >= N) {
       delete o;
       return fail("face index out of range");
     }

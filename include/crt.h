@@ -340,7 +340,10 @@ crt_status crt_batch_check(crt_batch* batch, void* stream);
  * Ka/Kd/Ks/Kt(Tf)/Ke/Ns with tinyobjloader's defaults.  Vertex and normal
  * coordinates are rounded to FP32 (crt_mesh_desc's precision).  The MTL is
  * looked up in mtl_dir (NULL: the OBJ's directory).  Every face corner must
- * carry a normal index (the reference reads normals[-1] otherwise).
+ * carry a normal index (the reference reads normals[-1] otherwise).  The
+ * file is parsed in chunks of whole lines on all host cores (environment
+ * variable CRT_OBJ_CHUNK_BYTES, default 262144, sets the chunk size; the
+ * result and the first error reported do not depend on it).
  * crt_obj_mesh points a mesh description at the loaded arrays (valid until
  * crt_obj_free). */
 typedef struct crt_obj crt_obj;

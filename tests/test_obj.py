@@ -114,3 +114,67 @@ def test_bmp_layout(tmp_path, built, w, h):
     crt.write_bmp(path, rgb, w, h)
     assert os.path.getsize(path) == 54 + h * (w * 3 + (-(w * 3) % 4))
     assert np.array_equal(read_bmp(path), rgb)
+
+
+def _load_chunked(path, chunk, monkeypatch):
+    import crt
+    monkeypatch.setenv("CRT_OBJ_CHUNK_BYTES", str(chunk))
+    return crt.load_obj_native(str(path), with_optics=True)
+
+
+def test_reader_result_does_not_depend_on_chunks(tmp_path, built, monkeypatch):
+    """The reader parses chunks of lines on all host cores; relative indices,
+    mtllib and usemtl lines, CRLF endings and a last line without a newline
+    read the same whatever the chunk boundaries (1 byte: every line its own
+    chunk)."""
+    (tmp_path / "scene.mtl").write_text(MTL)
+    (tmp_path / "late.mtl").write_text("newmtl late\nKd 0.1 0.9 0.1\nKs 0.3 0.3 0.3\nNi 1.2\n")
+    rng = np.random.default_rng(4)
+    lines = ["mtllib scene.mtl"]
+    nv = 0
+    for block in range(40):
+        for _ in range(6):
+            lines.append("v %.7g %.7g %.7g" % tuple(rng.normal(size=3)))
+            lines.append("vn %.7g %.7g %.7g" % tuple(rng.normal(size=3)))
+            nv += 1
+        if block == 11:
+            lines.append("usemtl red")
+        if block == 19:
+            lines.append("mtllib late.mtl\r")
+            lines.append("usemtl late")
+        if block == 27:
+            lines.append("usemtl")
+        if block == 33:
+            lines.append("usemtl glass")
+        lines.append("# block %d" % block)
+        lines.append("")
+        k = int(rng.integers(3, 7))
+        corners = ["%d//%d" % (-(j + 1), -(j + 1)) for j in range(k)]       # relative to this line
+        lines.append("f " + " ".join(corners) + ("\r" if block % 3 == 0 else ""))
+        i = int(rng.integers(1, nv + 1))
+        lines.append("f %d//%d %d//%d %d//%d" % (i, i, nv, nv, 1, 1))
+    text = "\n".join(lines)                                                     # no final newline
+    (tmp_path / "c.obj").write_text(text)
+    ref, ref_opt = _load_chunked(tmp_path / "c.obj", 1 << 30, monkeypatch)    # one chunk
+    assert ref.ntri > 100 and set(ref.matid.tolist()) == {0, 1, 2}
+    assert ref_opt.shape == (3, 4) and ref_opt[2, 3] == 1.2
+    for chunk in (1, 5, 37, 300, 4096):
+        got, opt = _load_chunked(tmp_path / "c.obj", chunk, monkeypatch)
+        for k in ("verts", "vidx", "normals", "nidx", "matid", "materials"):
+            assert np.array_equal(getattr(got, k), getattr(ref, k)), (chunk, k)
+        assert np.array_equal(opt, ref_opt), chunk
+
+
+@pytest.mark.parametrize("chunk", [1, 16, 1 << 30])
+def test_reader_reports_the_first_error_in_file_order(tmp_path, built, monkeypatch, chunk):
+    import crt
+    body = ["v 0 0 0", "v 1 0 0", "v 0 1 0", "vn 0 0 1"] + ["f 1//1 2//1 3//1"] * 30
+    body[20] = "f 1//1 2//1 x//1"        # line 21: a bad corner
+    body[30] = "v 1 2"                   # line 31: a bad vertex, later in the file
+    (tmp_path / "e.obj").write_text("\n".join(body) + "\n")
+    monkeypatch.setenv("CRT_OBJ_CHUNK_BYTES", str(chunk))
+    with pytest.raises(crt.CrtError, match="bad face corner at line 21$"):
+        crt.load_obj_native(str(tmp_path / "e.obj"))
+    (tmp_path / "big.obj").write_text("v 0 0 0\nvn 0 0 1\nf 1//1 1//1 4294967297//1\n")
+    with pytest.raises(crt.CrtError, match="bad face corner at line 3"):
+        crt.load_obj_native(str(tmp_path / "big.obj"))
