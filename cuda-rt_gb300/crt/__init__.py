@@ -135,16 +135,56 @@ def _check(status):
 
 
 def _addr(a):
-    """Address of a NumPy array or torch tensor (None -> NULL)."""
+    """Address of a contiguous NumPy array or torch tensor (None -> NULL)."""
     if a is None:
         return None
     if isinstance(a, np.ndarray):
-        assert a.flags["C_CONTIGUOUS"]
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("array is not C-contiguous")
         return a.ctypes.data
     if hasattr(a, "data_ptr"):
-        assert a.is_contiguous()
+        if not a.is_contiguous():
+            raise ValueError("tensor is not contiguous")
         return a.data_ptr()
     raise TypeError(type(a))
+
+
+def _kind(a):
+    """(kind, item size, element count) of a NumPy array or torch tensor;
+    kind is NumPy's letter: u unsigned, i signed, f floating point."""
+    if isinstance(a, np.ndarray):
+        return a.dtype.kind, a.dtype.itemsize, a.size
+    name = str(a.dtype).replace("torch.", "")
+    kind = "u" if name.startswith(("uint", "bool")) else "i" if name.startswith(("int", "long", "short")) else \
+        "f" if name.startswith(("float", "double", "half", "bfloat")) else "?"
+    return kind, a.element_size(), a.numel()
+
+
+def _need(a, name, kinds, itemsize, count):
+    """A caller's buffer that the library reads or writes `count` elements of:
+    the C ABI takes bare pointers, so type and size are checked here."""
+    if a is None:
+        return
+    k, size, n = _kind(a)
+    if k not in kinds or size != itemsize:
+        raise TypeError(f"{name}: {a.dtype} is not the {kinds[0]}{8 * itemsize} the library uses")
+    if n < count:
+        raise ValueError(f"{name}: {n} elements, {count} needed")
+
+
+# crt_render_out's buffers: (key, kinds, item size, elements per pixel, per sample, fixed)
+_RENDER_OUT = (("rgb8", "u", 1, 3, 0, 0), ("rgb_f32", "f", 4, 3, 0, 0), ("hit_id", "i", 4, 0, 1, 0),
+               ("hit_t", "f", 8, 0, 1, 0), ("shadow", "i", 4, 0, 1, 0), ("rays", "f", 8, 0, 6, 0),
+               ("traversal_stats", "ui", 8, 0, 0, 2), ("rgb_f64", "f", 8, 3, 0, 0), ("depth", "f", 8, 1, 0, 0),
+               ("shadow_id", "i", 4, 0, 1, 0))
+
+
+def _render_out(out, npx, ns):
+    """crt_render_out over the dict's buffers, each checked for its type and
+    for the full image's size (a row band writes at full-image indices)."""
+    for key, kinds, size, per_px, per_s, fixed in _RENDER_OUT:
+        _need(out.get(key), key, kinds, size, per_px * npx + per_s * ns + fixed)
+    return _RenderOut(*[_addr(out.get(k[0])) for k in _RENDER_OUT])
 
 
 def _stream(stream):
@@ -203,6 +243,7 @@ class Scene:
         """New vertex positions (None: a borrowing scene re-reads its own)."""
         if isinstance(verts, np.ndarray):
             verts = np.ascontiguousarray(verts, np.float32)
+        _need(verts, "vertices", "f", 4, 3 * self.nv)
         _check(lib().crt_scene_set_vertices(self.h, _addr(verts), int(bool(rebuild)), _stream(stream)))
 
     def build(self, stream=None):
@@ -228,6 +269,11 @@ class Scene:
         if out is None:
             out = dict(vertices=np.zeros((self.nv, 3), np.float64), light=np.zeros(3, np.float64),
                        kd=np.zeros((self.nmat, 3), np.float64))
+        npx = width * height
+        for a, name, count in ((grad_rgb, "grad_rgb", 3 * npx), (grad_depth, "grad_depth", npx),
+                               (out.get("vertices"), "vertices", 3 * self.nv), (out.get("light"), "light", 3),
+                               (out.get("kd"), "kd", 3 * self.nmat)):
+            _need(a, name, "f", 8, count)
         _check(lib().crt_adjoint_lambert(self.h, C.byref(cam), C.byref(lt), C.byref(p), _addr(grad_rgb),
                                          _addr(grad_depth), _addr(out.get("vertices")), _addr(out.get("light")),
                                          _addr(out.get("kd")), _stream(stream)))
@@ -251,6 +297,7 @@ class Scene:
             nrm = np.zeros((n, 3), np.float64) if normals and not any_hit else None
         else:
             import torch
+            _need(rays, "rays", "f", 8, 6 * n)
             ids = torch.empty(n, dtype=torch.int32, device=rays.device)
             t = torch.empty(n, dtype=torch.float64, device=rays.device)
             nrm = torch.empty((n, 3), dtype=torch.float64, device=rays.device) if normals and not any_hit else None
@@ -279,8 +326,7 @@ class Scene:
                            shadow=np.zeros(ns, np.int32), shadow_id=np.zeros(ns, np.int32))
             if rays:
                 out["rays"] = np.zeros((ns, 6), np.float64)
-        o = _RenderOut(*[_addr(out.get(k)) for k in ("rgb8", "rgb_f32", "hit_id", "hit_t", "shadow", "rays",
-                                                     "traversal_stats", "rgb_f64", "depth", "shadow_id")])
+        o = _render_out(out, width * height, width * height * spp)
         _check(lib().crt_render(self.h, C.byref(cam), C.byref(lt), C.byref(p), C.byref(o), _stream(stream)))
         return out
 
@@ -304,8 +350,8 @@ class Scene:
             op = optics  # None, or a device tensor of num_materials x 4 doubles
         else:
             op = np.ascontiguousarray(optics, np.float64).reshape(-1, 4)
-        o = _RenderOut(*[_addr(out.get(k)) for k in ("rgb8", "rgb_f32", "hit_id", "hit_t", "shadow", "rays",
-                                                     "traversal_stats", "rgb_f64", "depth", "shadow_id")])
+        _need(op, "optics", "f", 8, 4 * self.nmat)
+        o = _render_out(out, npx, ns)
         _check(lib().crt_render_recursive(self.h, C.byref(cam), C.byref(lt), C.byref(p), int(depth), _addr(op),
                                           C.byref(o), _stream(stream)))
         return out
@@ -362,6 +408,7 @@ class Batch:
     def run(self, out=None, graph=True, stream=None):
         """Build and render everything; `out` is a (total pixels, 3) uint8
         NumPy array or CUDA tensor, or None to keep the images on the device."""
+        _need(out, "out", "u", 1, 3 * sum(self.pixels))
         _check(lib().crt_batch_run(self.h, int(bool(graph)), _addr(out), _stream(stream)))
         return out
 
