@@ -1,4 +1,4 @@
-"""Generate logcabin_recorded.npz: the reference's one end-to-end result that
+"""Generate recorded/logcabin.npz: the reference's one end-to-end result that
 can be re-run from its checkout.
 
 The reference ships results/logcabin.bmp, rendered by its cuda_bvh on a
@@ -8,7 +8,9 @@ objs/funyz/logcabin.obj and .mtl.  This stores that scene (read with
 tinyobjloader's conventions, crt.data.load_obj), the flag values as the
 reference's main.cpp parses them (vectors through stof, scalars through
 stod) and the recorded image's pixels in the reference's bottom-up order.
-The GPU machine has no reference checkout; this file travels instead.
+It sits in its own folder: the fixtures beside this script all hold the
+build, trace and image dumps that the parity tests iterate over.  The GPU
+box has no reference checkout; this file travels instead.
 
 Run (in a container with the reference checkout):
     python tests/golden/make_logcabin.py
@@ -46,11 +48,11 @@ def main():
     w, h, rgb = read_recorded_bmp(os.path.join(REF, "results", "logcabin.bmp"))
     f = lambda *x: np.array([float(np.float32(v)) for v in x])  # noqa: E731  (stof)
     np.savez_compressed(
-        os.path.join(HERE, "logcabin_recorded.npz"), verts=mesh.verts, normals=mesh.normals, vidx=mesh.vidx,
+        os.path.join(HERE, "recorded", "logcabin.npz"), verts=mesh.verts, normals=mesh.normals, vidx=mesh.vidx,
         nidx=mesh.nidx, matid=mesh.matid, materials=mesh.materials, width=w, height=h, recorded_rgb=rgb,
         fov=35.0, fstop=16.0, focal_point=15.0, light_position=f(-4.0, 2.0, -4.0), light_color=f(1.0, 1.0, 1.0),
         light_radius=0.5, attenuation=f(0.0001, 0.0001, 0.01))
-    print("logcabin_recorded.npz:", mesh.ntri, "triangles,", w, "x", h)
+    print("recorded/logcabin.npz:", mesh.ntri, "triangles,", w, "x", h)
 
 
 if __name__ == "__main__":

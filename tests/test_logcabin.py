@@ -21,7 +21,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 def test_oracle_reproduces_the_recorded_logcabin_image(built):
     from crt import data
     from oracle.oracle import OracleScene
-    z = np.load(os.path.join(HERE, "golden", "logcabin_recorded.npz"))
+    z = np.load(os.path.join(HERE, "golden", "recorded", "logcabin.npz"))
     mesh = data.Mesh(z["verts"], z["vidx"], z["normals"], z["nidx"], z["matid"], z["materials"])
     cam = data.Camera(fov=float(z["fov"]), focal_point=float(z["focal_point"]), fstop=float(z["fstop"]))
     a = z["attenuation"]
