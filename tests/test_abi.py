@@ -1,6 +1,5 @@
 """The C ABI library loads and exports every entry point include/*.h declares
 (no compute calls: this runs without a GPU)."""
-import ctypes
 import glob
 import os
 import re

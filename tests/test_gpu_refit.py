@@ -4,7 +4,6 @@ reference rebuilds.  Closest hits do not depend on the tree (the candidate set
 is every triangle whose box and Moller-Trumbore test pass; only an exact t tie
 could be broken differently), so per-sample hit ids and t must match the
 oracle's full rebuild bit for bit at every checked frame."""
-import numpy as np
 import pytest
 
 from conftest import assert_equal
