@@ -242,7 +242,7 @@ crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* v
   for (int m = 0; m < M; m++) {
     const crt_batch_view& w = views[m];
     RenderArgs& a = ha[m];
-    std::memset(&a, 0, sizeof(a));
+    a = RenderArgs{};  // every field zero or null
     a.W = w.width, a.H = w.height, a.spp = w.spp, a.row0 = 0, a.row1 = w.height;
     a.angle = std::tan(M_PI * 0.5 * w.camera.fov / 180.0f);
     a.aspect = double(w.width) / double(w.height);
