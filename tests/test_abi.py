@@ -71,3 +71,50 @@ int main() {
                            str(src), "-L", lib, "-lcrt", "-Wl,-rpath," + lib, "-o", exe])
     r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0 and "cannot open" in r.stdout, (r.returncode, r.stdout, r.stderr)
+
+
+def test_cpp_wrappers_host_side(built, tmp_path):
+    """The host-only parts of include/crt.hpp: Scene::LoadObj fills the mesh
+    (fan-triangulated quad, Ks/Ni optics per material), and the classes
+    refuse calls made out of the reference's order (BVH of a scene without
+    setUpDevice, RayTracer::run before setUpDevice) with std::logic_error."""
+    import subprocess
+    (tmp_path / "q.mtl").write_text("newmtl m\nKd 0.5 0.5 0.5\nKs 0.25 0.5 0.75\nNi 1.33\n")
+    (tmp_path / "q.obj").write_text("mtllib q.mtl\nv 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nvn 0 0 1\n"
+                                    "usemtl m\nf 1//1 2//1 3//1 4//1\n")
+    src = tmp_path / "host.cpp"
+    src.write_text(r'''
+#include "crt.hpp"
+#include <cstdio>
+#include <stdexcept>
+int main(int argc, char** argv) {
+  (void)argc;
+  crt::Scene scene;
+  scene.LoadObj(argv[1]);
+  if (scene.numTriangles() != 2) return 2;
+  const std::vector<crt_optics> o = scene.optics();
+  if (o.size() != 1 || o[0].kr[0] != 0.25 || o[0].kr[2] != 0.75 || o[0].ior != 1.33) return 3;
+  try {
+    crt::BVH bvh(scene);
+    return 4;
+  } catch (const std::logic_error&) {
+  }
+  crt::RayTracer rt(16, 8, 1);
+  if (rt.width() != 16 || rt.height() != 8 || rt.image().size() != 16 * 8 * 3) return 5;
+  try {
+    rt.run();
+    return 6;
+  } catch (const std::logic_error&) {
+  }
+  crt::Scene moved = std::move(scene);
+  if (moved.numTriangles() != 2 || scene.numTriangles() != 0) return 7;
+  std::printf("ok\n");
+  return 0;
+}
+''')
+    lib = os.path.join(ROOT, "cuda-rt_gb300", "lib")
+    exe = str(tmp_path / "host")
+    subprocess.check_call(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                           str(src), "-L", lib, "-lcrt", "-Wl,-rpath," + lib, "-o", exe])
+    r = subprocess.run([exe, str(tmp_path / "q.obj")], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "ok" in r.stdout, (r.returncode, r.stdout, r.stderr)
