@@ -525,6 +525,24 @@ def run_next_rows(reps=3):
     return res
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu model")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
 def _cpu_impl():
     from oracle import oracle as orc
     kind = "port"
@@ -556,7 +574,7 @@ def cpu_baseline(sc, seconds):
         done += rows
         r0 = (r0 + 97) % (H - rows)
     value = done * W * spp / t_used / 1e6
-    return {"value": round(value, 4), "unit": "Mrays/s", "cores": cores, "kind": kind,
+    return {"value": round(value, 4), "unit": "Mrays/s", "cores": cores, "cpu_model": cpu_model(), "kind": kind,
             "sample": f"{done} rows of {W} px x {spp} spp (bands of 16 rows) of the {W}x{H} frame, "
                       f"BVH built once untimed, {t_used:.1f} s"}
 
@@ -588,8 +606,8 @@ def run_reference(args, dist, rank, ws):
             "config": {"workload": "large plain: nu=224 icosphere 1,003,520 tris FP32, 1920x1080 thin-lens render, "
                                    "Lambert + 1 shadow ray/hit (row-band sample)", "triangles": sc.mesh.ntri},
             "impl": "reference",
-            "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": cores, "kind": kind,
-                             "sample": sample},
+            "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": cores,
+                             "cpu_model": cpu_model(), "kind": kind, "sample": sample},
             "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 

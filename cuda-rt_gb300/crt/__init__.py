@@ -484,26 +484,61 @@ def render_args(camera, light, width, height, spp, rows=None, seed=0):
     return cam, lt, _RenderParams(width, height, spp, r0, r1, seed)
 
 
+def _need_words(a, name, count, allow_none=False):
+    """A 1-D array of 4-byte integers with at least `count` elements (the
+    stage entry points take bare device pointers to 32-bit words)."""
+    if a is None:
+        if allow_none:
+            return
+        raise ValueError(f"{name}: an array is required")
+    if len(a.shape) != 1:
+        raise ValueError(f"{name}: {len(a.shape)}-D, a 1-D array is required")
+    _need(a, name, "iu", 4, count)
+
+
 def morton(verts, vidx, scene_box, codes, stream=None):
     """crt_morton on device tensors."""
-    _check(lib().crt_morton(_addr(verts), int(verts.shape[0]), _addr(vidx), int(vidx.shape[0]), _addr(scene_box),
+    n = int(vidx.shape[0])
+    _need(verts, "verts", "f", 4, 3 * int(verts.shape[0]))
+    _need(vidx, "vidx", "i", 4, 3 * n)
+    _need(scene_box, "scene_box", "f", 4, 6)
+    _need_words(codes, "codes", n)
+    _check(lib().crt_morton(_addr(verts), int(verts.shape[0]), _addr(vidx), n, _addr(scene_box),
                             _addr(codes), _stream(stream)))
 
 
+def _sort_args(keys_in, vals_in, keys_out, vals_out):
+    _need_words(keys_in, "keys_in", 0)
+    n = int(keys_in.shape[0])
+    _need_words(vals_in, "vals_in", n, allow_none=True)
+    _need_words(keys_out, "keys_out", n)
+    _need_words(vals_out, "vals_out", n)
+    return n
+
+
 def sort_pairs(keys_in, vals_in, keys_out, vals_out, key_bits=32, stream=None):
-    """crt_sort_pairs on device tensors (stable LSD radix sort)."""
-    _check(lib().crt_sort_pairs(_addr(keys_in), _addr(vals_in), _addr(keys_out), _addr(vals_out),
-                                int(keys_in.shape[0]), key_bits, _stream(stream)))
+    """crt_sort_pairs on device tensors (stable LSD radix sort; 1-D 32-bit
+    integer arrays, outputs at least as long as keys_in, no overlap)."""
+    n = _sort_args(keys_in, vals_in, keys_out, vals_out)
+    _check(lib().crt_sort_pairs(_addr(keys_in), _addr(vals_in), _addr(keys_out), _addr(vals_out), n, key_bits,
+                                _stream(stream)))
 
 
 def sort_pairs_noalloc(keys_in, vals_in, keys_out, vals_out, key_bits=32, stream=None):
     """crt_sort_pairs_noalloc on device tensors: the same sort with its scratch
     in a fixed device array (at most CRT_SORT_NOALLOC_MAX_PAIRS pairs)."""
-    _check(lib().crt_sort_pairs_noalloc(_addr(keys_in), _addr(vals_in), _addr(keys_out), _addr(vals_out),
-                                        int(keys_in.shape[0]), key_bits, _stream(stream)))
+    n = _sort_args(keys_in, vals_in, keys_out, vals_out)
+    _check(lib().crt_sort_pairs_noalloc(_addr(keys_in), _addr(vals_in), _addr(keys_out), _addr(vals_out), n,
+                                        key_bits, _stream(stream)))
 
 
 SORT_NOALLOC_MAX_PAIRS = 1 << 20
+
+# The component of the area-light offset that each of the three light draws
+# of a hit goes to (first, second, third draw): the order in which nvcc
+# evaluates randVec3d's constructor arguments in the reference
+# (kernels/mrand.cu:33-35), which the pixel kernels follow.
+LIGHT_DRAW_ORDER = (0, 1, 2)
 
 
 def camera_angle(fov):

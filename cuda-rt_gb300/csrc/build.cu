@@ -1338,6 +1338,39 @@ cudaError_t launch_morton(const float* verts, int nv, const int* vidx, int n, co
   return cudaGetLastError();
 }
 
+namespace {
+bool on_current_device(const void* p, int dev) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) && a.device == dev;
+}
+bool overlap(const void* a, const void* b, size_t bytes) {
+  const uintptr_t x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
+  return x < y + bytes && y < x + bytes;
+}
+}  // namespace
+
+const char* sort_args_problem(const uint32_t* kin, const uint32_t* vin, const uint32_t* kout, const uint32_t* vout,
+                              int n) {
+  if (!kin || !kout || !vout) return "null array";
+  const size_t bytes = sizeof(uint32_t) * (size_t)n;
+  if (overlap(kin, kout, bytes) || overlap(kin, vout, bytes) || overlap(kout, vout, bytes) ||
+      (vin && (overlap(vin, kout, bytes) || overlap(vin, vout, bytes))))
+    return "the sort's input and output arrays overlap (it does not sort in place)";
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return "no current CUDA device";
+  }
+  if (!(on_current_device(kin, dev) && on_current_device(kout, dev) && on_current_device(vout, dev) &&
+        (!vin || on_current_device(vin, dev))))
+    return "the sort takes device pointers on the current device";
+  return nullptr;
+}
+
 // Scratch layout: [tmp keys n][tmp vals n][hist passes*R][status passes*tiles*R][counters 4][err 1]
 size_t sort_scratch_bytes(int n, int key_bits) {
   const int passes = sort_passes(key_bits);

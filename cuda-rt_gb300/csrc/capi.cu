@@ -694,9 +694,8 @@ crt_status crt_sort_pairs(const uint32_t* kin, const uint32_t* vin, uint32_t* ko
                           int32_t key_bits, void* stream) {
   if (n < 0 || n > CRT_MAX_TRIANGLES || key_bits < 1 || key_bits > 32) return fail(CRT_INVALID_ARG, "bad sizes");
   if (n == 0) return CRT_OK;
-  if (!kin || !kout || !vout) return fail(CRT_INVALID_ARG, "null array");
-  if (!(is_device_ptr(kin) && is_device_ptr(kout) && is_device_ptr(vout) && (!vin || is_device_ptr(vin))))
-    return fail(CRT_INVALID_ARG, "crt_sort_pairs takes device pointers");
+  if (const char* why = sort_args_problem(kin, vin, kout, vout, n))
+    return fail(CRT_INVALID_ARG, std::string("crt_sort_pairs: ") + why);
   cudaStream_t st = S(stream);
   const size_t bytes = sort_scratch_bytes(n, key_bits) + 256;
   void* scratch = nullptr;

@@ -87,6 +87,13 @@ cudaError_t launch_morton(const float* verts, int nv, const int* vidx, int n, co
                           int* err, cudaStream_t st);
 // Stable LSD radix sort; scratch holds sort_scratch_bytes(n, key_bits).
 size_t sort_scratch_bytes(int n, int key_bits);
+// Argument check shared by crt_sort_pairs and crt_sort_pairs_noalloc (n > 0):
+// every array in device memory of the current device, and no input array
+// overlapping an output array, nor the two outputs each other (pass 0 of a
+// multi-pass sort writes an output while later tiles still read the input).
+// Returns NULL when the arguments are usable, else what is wrong.
+const char* sort_args_problem(const uint32_t* kin, const uint32_t* vin, const uint32_t* kout, const uint32_t* vout,
+                              int n);
 cudaError_t launch_sort_pairs(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, int n,
                               int key_bits, void* scratch, int* err, cudaStream_t st);
 

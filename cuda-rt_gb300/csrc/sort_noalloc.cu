@@ -16,6 +16,15 @@
 // (histograms, tile counters, look-back status, error flag), and two calls
 // whose work overlaps on the GPU (different streams, no ordering between
 // them) race on it.
+//
+// Set-up: host code cannot pass the array's name to a kernel (in host code it
+// names a host-side stand-in), so the first call in each CUDA context (per
+// device, and again after cudaDeviceReset gives the device a new context)
+// looks up its device address with cudaGetSymbolAddress while that device is
+// current.  With lazy module loading that first lookup also loads this
+// library's device code onto the device, which is when the array's memory is
+// taken: make the first call at initialisation (it can fail there with an
+// out-of-memory error) and before any stream capture.
 #include <mutex>
 
 #include "crt.h"
@@ -39,34 +48,57 @@ static __device__ __align__(256) unsigned char g_sort_scratch[kNoAllocScratchByt
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-void* g_scratch_addr[kMaxDevices] = {};
+struct ScratchAddr {
+  unsigned long long ctx_id = 0;  // the CUDA context the address belongs to
+  void* addr = nullptr;
+};
+ScratchAddr g_scratch_addr[kMaxDevices];
 
-// The device address of g_sort_scratch on the current device, looked up once
-// per device with that device current.  The array's name in host code is only
-// a host-side handle; passing it to a kernel would fault.
+// cuCtxGetCurrent and cuCtxGetId through the runtime's driver entry points
+// (no link-time dependence on libcuda): a context's id is unique for the
+// life of the process, so an address looked up in a context that
+// cudaDeviceReset has since destroyed is never reused.
+typedef int (*CtxGetCurrentFn)(void** ctx);
+typedef int (*CtxGetIdFn)(void* ctx, unsigned long long* id);
+void* driver_fn(const char* name) {
+  void* f = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion(name, &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return f;
+}
+bool current_context_id(unsigned long long* id) {
+  static CtxGetCurrentFn get_current = reinterpret_cast<CtxGetCurrentFn>(driver_fn("cuCtxGetCurrent"));
+  static CtxGetIdFn get_id = reinterpret_cast<CtxGetIdFn>(driver_fn("cuCtxGetId"));
+  void* ctx = nullptr;
+  return get_current && get_id && get_current(&ctx) == 0 && ctx && get_id(ctx, id) == 0;
+}
+
+// The device address of g_sort_scratch in the current context, looked up
+// once per context with its device current.
 cudaError_t scratch_on_current_device(void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  e = cudaSetDevice(dev);  // initialises the device's primary context and makes it current
+  if (e != cudaSuccess) return e;
+  unsigned long long id = 0;
+  if (!current_context_id(&id)) return cudaErrorInitializationError;
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_addr[dev]) {
+  ScratchAddr& c = g_scratch_addr[dev];
+  if (!c.addr || c.ctx_id != id) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_sort_scratch);
     if (e != cudaSuccess) return e;
-    g_scratch_addr[dev] = p;
+    c.addr = p;
+    c.ctx_id = id;
   }
-  *out = g_scratch_addr[dev];
+  *out = c.addr;
   return cudaSuccess;
-}
-
-bool on_device(const void* p) {
-  cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
 crt_status fail(crt_status s, const char* msg) {
@@ -82,9 +114,7 @@ extern "C" crt_status crt_sort_pairs_noalloc(const uint32_t* kin, const uint32_t
   if ((size_t)n > kMaxPairs)
     return fail(CRT_INVALID_ARG, "crt_sort_pairs_noalloc: more than CRT_SORT_NOALLOC_MAX_PAIRS pairs");
   if (n == 0) return CRT_OK;
-  if (!kin || !kout || !vout) return fail(CRT_INVALID_ARG, "null array");
-  if (!(on_device(kin) && on_device(kout) && on_device(vout) && (!vin || on_device(vin))))
-    return fail(CRT_INVALID_ARG, "crt_sort_pairs_noalloc takes device pointers");
+  if (const char* why = crt::sort_args_problem(kin, vin, kout, vout, n)) return fail(CRT_INVALID_ARG, why);
   void* scratch = nullptr;
   cudaError_t e = scratch_on_current_device(&scratch);
   if (e != cudaSuccess) {

@@ -170,7 +170,11 @@ crt_status crt_trace_shadow(crt_scene* scene, const double* rays, int64_t n, int
 /* ---- render: RayTracer::run + pullRaytracedImage (kernels/raytracer.cu:55-166,
  * inc/raytracer.h:53-63): thin-lens primary rays on the mrand stream,
  * closest hit, Material::shade with one shadow ray per hit, mean over the
- * samples, clamp, quantise. */
+ * samples, clamp, quantise.  Device memory: the first thin-lens render on a
+ * device (finite fstop) also builds that device's thin-lens tables, 2.0 GB
+ * held until the process exits, when 8 GB are free and no stream capture is
+ * under way (see crt_set_lens_tables; crt_set_lens_tables(0) beforehand
+ * keeps them off). */
 crt_status crt_render(crt_scene* scene, const crt_camera* camera, const crt_light* light,
                       const crt_render_params* params, const crt_render_out* out, void* stream);
 
@@ -256,8 +260,10 @@ crt_status crt_refit(const float* vertices, int32_t num_vertices, const int32_t*
                      const uint32_t* ids, const int32_t* nodes3, float* node_boxes, void* stream);
 /* Stable ascending LSD radix sort of (key, value) pairs on the low
  * `key_bits` bits of the keys (thrust::sort_by_key, kernels/bvh.cu:267-273).
- * vals_in may be NULL: values are then 0..n-1.  In and out arrays must not
- * overlap.  Scratch is allocated per call (cudaMallocAsync); the call
+ * vals_in may be NULL: values are then 0..n-1.  Device pointers of the
+ * current device.  It does not sort in place: an input array that overlaps
+ * an output array, or two overlapping outputs, are refused with
+ * CRT_INVALID_ARG.  Scratch is allocated per call (cudaMallocAsync); the call
  * synchronises `stream` and reports a look-back timeout as CRT_TIMEOUT. */
 crt_status crt_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out,
                           int32_t n, int32_t key_bits, void* stream);
@@ -271,11 +277,16 @@ crt_status crt_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint
  * 16.8 MB inside libcrt.so, held on every GPU that loads the library until
  * the process exits; n may not exceed CRT_SORT_NOALLOC_MAX_PAIRS (larger n:
  * CRT_INVALID_ARG, nothing launched).  No cudaMalloc/cudaFree or other
- * allocating call is made.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress) with that device current; make that
- * first call before any stream capture.  All calls share the array: each
- * clears what must start at zero, and calls whose work overlaps on the GPU
- * race.  Device pointers only; synchronises `stream`. */
+ * allocating call is made.  The first call in each CUDA context (per device,
+ * and again after cudaDeviceReset) looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; with lazy module loading
+ * that lookup also loads the library's device code, which places the array,
+ * so the first call can fail with an out-of-memory CRT_CUDA_ERROR: make it at
+ * initialisation, and before any stream capture.  All calls share the array:
+ * each clears what must start at zero, and calls whose work overlaps on the
+ * GPU race.  As crt_sort_pairs: device pointers of the current device, no
+ * overlap between an input and an output array or between the outputs
+ * (CRT_INVALID_ARG); synchronises `stream`. */
 #define CRT_SORT_NOALLOC_MAX_PAIRS (1 << 20)
 crt_status crt_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                                   uint32_t* vals_out, int32_t n, int32_t key_bits, void* stream);

@@ -390,9 +390,33 @@ inline double rand_double(uint32_t& st) {
   return (double)((float)v * 1.0 / 4294967296.0);
 }
 
+// randVec3d (kernels/mrand.cu:33-35) is Vec3d(randDouble(), randDouble(),
+// randDouble()): the order in which a compiler evaluates the three
+// constructor arguments decides which draw lands in which component.
+// g_light_order[i] is the component that the i-th draw goes to ({0, 1, 2}:
+// left to right).
+int g_light_order[3] = {0, 1, 2};
+inline void light_draws(uint32_t& st, double r[3]) {
+  for (int i = 0; i < 3; i++) r[g_light_order[i]] = rand_double(st);
+}
+
 }  // namespace
 
 extern "C" {
+
+// Which component each of randVec3d's three draws goes to (a permutation of
+// 0, 1, 2); returns -1 and changes nothing for anything else.
+int orc_set_light_draw_order(int first, int second, int third) {
+  const int o[3] = {first, second, third};
+  int seen = 0;
+  for (int i = 0; i < 3; i++) {
+    if (o[i] < 0 || o[i] > 2) return -1;
+    seen |= 1 << o[i];
+  }
+  if (seen != 7) return -1;
+  for (int i = 0; i < 3; i++) g_light_order[i] = o[i];
+  return 0;
+}
 
 struct orc_material {  // one reference Material (inc/material.h:8-24), the fields shade() reads
   double ka[3], kd[3], ks[3], kt[3], ke[3];
@@ -430,10 +454,9 @@ static V3 shade_hit(const Scene& s, const orc_camera* cam, const orc_light* ligh
   V3 Vv = eye - q;
   Vv = v3(-Vv.x, -Vv.y, -Vv.z);
   Vv = normalize(Vv);
-  double r0 = rand_double(st);
-  double r1 = rand_double(st);
-  double r2 = rand_double(st);
-  V3 off = v3(r0, r1, r2) * light->radius;
+  double r[3];
+  light_draws(st, r);
+  V3 off = v3(r[0], r[1], r[2]) * light->radius;
   off = v3(off.x - 0.5, off.y - 0.5, off.z - 0.5);
   V3 L = normalize(lpos + off - q);
   double dist = norm(lpos - q);
@@ -872,8 +895,9 @@ void orc_adjoint(void* h, const orc_camera* cam, const orc_light* light, int W, 
         V3 Nr = (1.0 - (hh.alpha + hh.beta)) * nA + hh.alpha * nB + hh.beta * nC;
         double sN = 1.0 / (double)sqrtf((float)(Nr.x * Nr.x + Nr.y * Nr.y + Nr.z * Nr.z));
         V3 N = Nr * sN;
-        double r0 = rand_double(st), r1 = rand_double(st), r2 = rand_double(st);
-        V3 off = v3(r0 * light->radius - 0.5, r1 * light->radius - 0.5, r2 * light->radius - 0.5);
+        double r[3];
+        light_draws(st, r);
+        V3 off = v3(r[0] * light->radius - 0.5, r[1] * light->radius - 0.5, r[2] * light->radius - 0.5);
         V3 Lp = lpos + off - q;
         double sL = 1.0 / (double)sqrtf((float)(Lp.x * Lp.x + Lp.y * Lp.y + Lp.z * Lp.z));
         V3 L = Lp * sL;

@@ -48,8 +48,13 @@ PIECES = [
 ]
 
 
+# Where this container mounts the reference checkout; CRT_REFERENCE_DIR
+# overrides it.  Every script that reads the reference's sources asks here.
+REFERENCE_CHECKOUT = "/root/reference"
+
+
 def default_reference():
-    return os.environ.get("CRT_REFERENCE_DIR", "/root/reference")
+    return os.environ.get("CRT_REFERENCE_DIR", REFERENCE_CHECKOUT)
 
 
 def extract(ref, rel, ranges):

@@ -30,7 +30,9 @@ sys.path.insert(0, os.path.join(ROOT, "cuda-rt_gb300"))
 from crt import data  # noqa: E402
 from oracle.oracle import OracleScene, ref_available  # noqa: E402
 
-REF = os.environ.get("CRT_REFERENCE_DIR", "/root/reference")
+from oracle.ref.build_ref import default_reference  # noqa: E402
+
+REF = default_reference()
 
 OBJ_FIXTURES = ["testyz/bvh_simple1", "testyz/bvh_simple2", "testyz/bvh_simple3", "testyz/bvh_simple4",
                 "testyz/bvh_simple5", "testyz/bvh_simple6", "testyz/oneplane", "testyz/oneplane2",

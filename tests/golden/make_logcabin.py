@@ -27,7 +27,10 @@ sys.path.insert(0, os.path.join(ROOT, "cuda-rt_gb300"))
 
 from crt import data  # noqa: E402
 
-REF = os.environ.get("CRT_REFERENCE_DIR", "/root/reference")
+sys.path.insert(0, ROOT)
+from oracle.ref.build_ref import default_reference  # noqa: E402
+
+REF = default_reference()
 
 
 def read_recorded_bmp(path):

@@ -133,3 +133,25 @@ def test_batch_create_refuses_oversized_meshes_and_views(lib):
     d, keep = _big_desc(1 << 28, 3)
     assert attempt(d, m=3) == INVALID and "batch mesh 2" in error(lib)
     assert not out.value
+
+
+def test_sort_refuses_overlapping_arrays(lib):
+    """The sort does not work in place: pass 0 of a multi-pass sort writes an
+    output while later tiles still read the input.  Overlapping ranges are
+    refused before any CUDA call (these addresses are never dereferenced)."""
+    base = 1 << 40
+    n = 1000
+    cases = [
+        (base, None, base + 4 * (n - 1), base + 8 * n),  # keys_out starts inside keys_in
+        (base, None, base + 8 * n, base + 4 * 10),  # vals_out inside keys_in
+        (base, base + 8 * n, base + 16 * n, base + 8 * n + 4),  # vals_out inside vals_in
+        (base, None, base + 8 * n, base + 8 * n + 4),  # the two outputs overlap
+    ]
+    for f in (lib.crt_sort_pairs, lib.crt_sort_pairs_noalloc):
+        for kin, vin, kout, vout in cases:
+            assert f(kin, vin, kout, vout, n, 30, None) == INVALID
+            assert b"overlap" in lib.crt_last_error_string()
+    # adjacent, non-overlapping ranges get past this check (and stop at the
+    # device-pointer check: these are not device addresses)
+    assert lib.crt_sort_pairs(base, None, base + 4 * n, base + 8 * n, n, 30, None) == INVALID
+    assert b"overlap" not in lib.crt_last_error_string()

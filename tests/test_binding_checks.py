@@ -64,3 +64,31 @@ def test_torch_tensors_are_checked_too(scene):
         scene.render(cam, light, 8, 4, 1, out={"hit_id": torch.zeros(32, dtype=torch.int64)})
     with pytest.raises(ValueError, match="rgb_f64"):
         scene.render(cam, light, 8, 4, 1, out={"rgb_f64": torch.zeros((31, 3), dtype=torch.float64)})
+
+
+def test_sort_and_morton_buffers(built):
+    """crt_sort_pairs(_noalloc) and crt_morton write n 32-bit words through
+    bare pointers: 1-D 4-byte integer arrays of at least n elements only."""
+    import crt
+    torch = pytest.importorskip("torch")
+    k = torch.zeros(64, dtype=torch.int32)
+    for f in (crt.sort_pairs, crt.sort_pairs_noalloc):
+        with pytest.raises(ValueError, match="keys_out: 63 elements, 64 needed"):
+            f(k, None, torch.zeros(63, dtype=torch.int32), torch.zeros(64, dtype=torch.int32))
+        with pytest.raises(ValueError, match="vals_out"):
+            f(k, None, torch.zeros(64, dtype=torch.int32), torch.zeros(10, dtype=torch.int32))
+        with pytest.raises(ValueError, match="vals_in"):
+            f(k, torch.zeros(32, dtype=torch.int32), torch.zeros(64, dtype=torch.int32),
+              torch.zeros(64, dtype=torch.int32))
+        with pytest.raises(TypeError, match="keys_out"):
+            f(k, None, torch.zeros(64, dtype=torch.int64), torch.zeros(64, dtype=torch.int32))
+        with pytest.raises(TypeError, match="keys_in"):
+            f(torch.zeros(64, dtype=torch.float32), None, k.clone(), k.clone())
+        with pytest.raises(ValueError, match="1-D"):
+            f(torch.zeros((8, 8), dtype=torch.int32), None, k.clone(), k.clone())
+    with pytest.raises(ValueError, match="codes: 9 elements, 10 needed"):
+        crt.morton(torch.zeros((5, 3)), torch.zeros((10, 3), dtype=torch.int32), torch.zeros(6),
+                   torch.zeros(9, dtype=torch.int32))
+    with pytest.raises(TypeError, match="vidx"):
+        crt.morton(torch.zeros((5, 3)), torch.zeros((10, 3), dtype=torch.int64), torch.zeros(6),
+                   torch.zeros(10, dtype=torch.int32))

@@ -1,0 +1,159 @@
+"""Parity at the benchmark workloads' own sizes.
+
+The other GPU tests check the pixel kernel on reduced images; the mrand seed
+of a pixel is the wangHash of its thread id in the reference's 16x16-block
+launch over a W/16-wide grid (inc/indexing.h:4-9, kernels/raytracer.cu:106),
+and the kernel's tiles and sample-parallel speculation depend on W, H and
+the tile shape, so here the frames that bench.py times are rendered whole
+and compared with the oracle:
+
+* the large plain frame: 1,003,520 faces, 1920x1080 at 16 spp, thin lens
+  (1080 rows: the top band of the seed grid, rows 1072-1079, is partial);
+* one frame of the refit workload, 1280x720 at 4 spp after 30 refits on
+  frame 0's topology;
+* the batched workload (256 meshes, 1k-500k triangles, 256x256 at 4 spp)
+  through crt_batch_*: every mesh's image equals the plain path's, and the
+  largest mesh's build products and image equal the oracle's.
+
+Thin-lens rays use CUDA's double cos/sin, which may differ from the host
+libm's in the last bit, so the oracle replays the GPU's primary rays; after
+that, hit ids, t, shadow bits and 8-bit pixels are compared bit for bit.
+"""
+import numpy as np
+import pytest
+
+from conftest import assert_equal
+
+pytestmark = pytest.mark.gpu
+
+
+def _ulp_close(a, b, ulps=4):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    tol = ulps * np.spacing(np.maximum(np.abs(a), np.abs(b)))
+    return np.abs(a - b) <= np.maximum(tol, 1e-300)
+
+
+def _rows(img, W, H):
+    """(H, W, 3) in top-down row order (memory rows are bottom-up)."""
+    return img.reshape(H, W, 3)[::-1]
+
+
+def test_large_frame_full_size(cuda):
+    """The bench's timed frame, whole: build + render exactly as bench.py does
+    (device image only), then the same render with every per-sample output,
+    then the oracle replaying all 33 M primary rays."""
+    import crt
+    from crt import data
+    from oracle.oracle import OracleScene
+    torch = cuda
+    sc = data.config1()
+    W, H, spp = sc.width, sc.height, sc.spp
+    assert (W, H, spp) == (1920, 1080, 16)
+    g = crt.Scene(sc.mesh)
+    # as timed: rebuild from the resident vertices, render into a device image
+    g.build()
+    dev = torch.empty((W * H, 3), dtype=torch.uint8, device="cuda")
+    g.render(sc.camera, sc.light, W, H, spp, out={"rgb8": dev})
+    torch.cuda.synchronize()
+    timed = dev.cpu().numpy()
+    out = g.render(sc.camera, sc.light, W, H, spp, aux=True, rays=True)
+    g.check()
+    assert_equal(out["rgb8"], timed, "rgb8 of the timed call vs the call with per-sample outputs")
+    o = OracleScene(sc.mesh)
+    rep = o.render(sc.camera, sc.light, W, H, spp=spp, rays_in=out["rays"], aux=True)
+    assert_equal(out["hit_id"], rep["hit_id"], "hit id")
+    assert np.array_equal(out["hit_t"], rep["hit_t"]), "hit t"
+    assert_equal(out["shadow"], rep["shadow"], "shadow")
+    assert_equal(out["rgb8"], rep["rgb"], "rgb8")
+    # the partial top band of the 16-row seed grid, and two full bands, with
+    # the oracle's own rays (host libm): rays within 4 ulp for > 99%
+    for r0, r1 in ((1072, 1080), (0, 16), (528, 544)):
+        own = o.render(sc.camera, sc.light, W, H, spp=spp, rows=(r0, r1), rays_out=True, aux=True)
+        sel = np.zeros((H, W * spp), bool)
+        sel[r0:r1] = True
+        sel = sel[::-1].reshape(-1)  # sample index order: bottom-up rows, then x, then sample
+        close = _ulp_close(out["rays"][sel], own["rays"][sel]).all(1)
+        assert close.mean() > 0.99, f"rows {r0}-{r1}: {(~close).sum()} rays beyond 4 ulp"
+        d = np.abs(_rows(out["rgb8"], W, H)[r0:r1].astype(int) - _rows(own["rgb"], W, H)[r0:r1].astype(int))
+        assert d.max() <= 1 or (d > 0).mean() < 1e-3, f"rows {r0}-{r1}: max {d.max()}"
+    hits = out["hit_id"] >= 0
+    assert 0.1 < hits.mean() < 0.9
+    top = _rows(out["rgb8"], W, H)[1072:1080]
+    assert top.shape == (8, W, 3)
+
+
+def test_refit_frame_full_size(cuda):
+    """The refit workload at its own size: frame 30 after 30 refits on frame
+    0's topology.  Against the oracle refitted on the same topology every
+    output is bit-exact (the shadow ray's first hit in DFS order depends on
+    the tree); against the oracle's full rebuild the closest hits (which do
+    not depend on the tree) are."""
+    import crt
+    from crt import data
+    from oracle.oracle import OracleScene
+    anim = data.Animation()
+    sc = anim.scene()
+    W, H, spp = sc.width, sc.height, sc.spp
+    assert (W, H, spp) == (1280, 720, 4)
+    g = crt.Scene(anim.mesh0)
+    for f in range(1, 31):
+        g.set_vertices(anim.vertices(f), rebuild=False)
+    out = g.render(sc.camera, sc.light, W, H, spp, aux=True, rays=True)
+    g.check()
+    o = OracleScene(anim.mesh0)
+    o.set_vertices(anim.vertices(30), rebuild=False)  # a refit depends on the topology and vertices only
+    ref = o.render(sc.camera, sc.light, W, H, spp=spp, rays_in=out["rays"], aux=True)
+    assert_equal(out["hit_id"], ref["hit_id"], "hit id (refit)")
+    assert np.array_equal(out["hit_t"], ref["hit_t"]), "hit t (refit)"
+    assert_equal(out["shadow"], ref["shadow"], "shadow (refit)")
+    assert_equal(out["rgb8"], ref["rgb"], "rgb8 (refit)")
+    o.set_vertices(anim.vertices(30), rebuild=True)
+    reb = o.render(sc.camera, sc.light, W, H, spp=spp, rays_in=out["rays"], aux=True)
+    assert_equal(out["hit_id"], reb["hit_id"], "hit id (rebuild)")
+    assert np.array_equal(out["hit_t"], reb["hit_t"]), "hit t (rebuild)"
+    assert (out["hit_id"] >= 0).mean() > 0.1
+
+
+def test_batched_workload_full_size(cuda):
+    """The batched workload as bench.py runs it (256 meshes, graph replay,
+    autotuned shape): every mesh's image equals the plain path's for that
+    mesh alone; the largest mesh (~500k triangles), the smallest and one in
+    between are checked against the oracle (build products bit-exact, image
+    bit-exact on the plain path's replayed rays)."""
+    import crt
+    from crt import data
+    from oracle.oracle import OracleScene
+    torch = cuda
+    scs = data.config3()
+    assert len(scs) == 256
+    views = [(s.camera, s.light, s.width, s.height, s.spp) for s in scs]
+    b = crt.Batch([s.mesh for s in scs], views)
+    total = int(b.offsets[-1])
+    img = torch.empty((total, 3), dtype=torch.uint8, device="cuda")
+    b.autotune()
+    b.run(img, graph=True)
+    b.run(img, graph=True)
+    torch.cuda.synchronize()
+    b.check()
+    imgs = b.images(img.cpu().numpy())
+    sizes = [s.mesh.ntri for s in scs]
+    big, small = int(np.argmax(sizes)), int(np.argmin(sizes))
+    mid = int(np.argsort(sizes)[len(sizes) // 2])
+    assert sizes[big] > 400_000
+    for m, s in enumerate(scs):
+        p = crt.Scene(s.mesh)
+        check = m in (big, small, mid)
+        res = p.render(s.camera, s.light, s.width, s.height, s.spp, aux=check, rays=check)
+        assert_equal(imgs[m], res["rgb8"], f"mesh {m} ({sizes[m]} tris): batched vs plain image")
+        if check:
+            o = OracleScene(s.mesh)
+            e, r = b.export(m), o.export()
+            for k in ("codes", "ids", "nodes", "node_boxes"):
+                assert_equal(e[k], r[k], f"mesh {m} {k}")
+            rep = o.render(s.camera, s.light, s.width, s.height, spp=s.spp, rays_in=res["rays"], aux=True)
+            assert_equal(res["hit_id"], rep["hit_id"], f"mesh {m} hit id")
+            assert_equal(res["shadow"], rep["shadow"], f"mesh {m} shadow")
+            assert_equal(imgs[m], rep["rgb"], f"mesh {m} batched image vs oracle")
+        p.check()
+        p.close()
+    b.close()

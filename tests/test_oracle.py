@@ -113,3 +113,30 @@ def test_oracle_light_offset_convention():
     p = data.light_for((2.0, 2.0, -2.0), (0.0, 0.0, -3.0))
     assert p == (-1.5, 2.5, -0.5)
     assert math.isclose(data.view_transform(np.array([[0.0, 0.0, 0.0]]), (0, 0, -3))[0, 2], -3.0)
+
+
+@pytest.mark.skipif(not ref_available(), reason="oracle/_ref not built (no reference checkout here)")
+def test_area_light_draw_order_of_the_host_compiled_reference():
+    """randVec3d's three draws (kernels/mrand.cu:33-35) are constructor
+    arguments, whose evaluation order C++ leaves to the compiler.  The
+    reference compiled for the host by g++ takes them right to left (the
+    first draw lands in z): with an area light its image equals the oracle's
+    with that order and differs from every other order.  (The GPU order is
+    nvcc's, checked by tests/test_gpu_draw_order.py.)"""
+    import itertools
+    sc = data.config0(n=3000, width=48, height=32)
+    light = data.Light(position=sc.light.position, radius=0.7)
+    ref = OracleScene(sc.mesh, "ref").render(sc.camera, light, 48, 32)
+    o = OracleScene(sc.mesh)
+    try:
+        same = []
+        for perm in itertools.permutations(range(3)):
+            assert o.lib.orc_set_light_draw_order(*perm) == 0
+            out = o.render(sc.camera, light, 48, 32, spp=20)
+            if np.array_equal(out["color"], ref["color"]):
+                same.append(perm)
+    finally:
+        import crt
+        o.lib.orc_set_light_draw_order(*crt.LIGHT_DRAW_ORDER)
+    assert same == [(2, 1, 0)], same
+    assert o.lib.orc_set_light_draw_order(0, 0, 1) == -1
