@@ -21,6 +21,17 @@ namespace {
 
 constexpr int kSpinLimit = 1 << 20;  // bounded look-back wait (x ~64 ns)
 
+// Programmatic dependent launch.  The plain build launches its kernels as
+// programmatic dependents of the kernel before them (launch_dep): a
+// dependent's blocks may be scheduled once every block of the kernel before
+// it has started, and pdl_wait() holds them until that kernel has completed
+// and its writes are visible.  Every build kernel calls pdl_wait() before it
+// touches global memory and then lets its own dependents be scheduled, so a
+// stage boundary no longer costs a launch.  Launched the ordinary way, both
+// instructions are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
+
 __device__ __forceinline__ void tri_box(const float* __restrict__ V, const int* __restrict__ vidx, int t,
                                         float3& a, float3& b, float3& c, float lo[3], float hi[3]) {
   const int ia = __ldg(vidx + 3 * t), ib = __ldg(vidx + 3 * t + 1), ic = __ldg(vidx + 3 * t + 2);
@@ -45,6 +56,8 @@ __device__ __forceinline__ bool finite_coords(float3 a, float3 b, float3 c) {
 }
 
 __global__ void k_build_init(SceneGlobals* g, uint32_t* hist, int nhist) {
+  pdl_wait();
+  pdl_launch_dependents();
   const int t = threadIdx.x;
   if (t < 3) {
     g->bmin[t] = f2ord(1e9f);  // findMinMax's initial values (kernels/scene.cu:75,80)
@@ -62,6 +75,8 @@ __global__ void k_build_init(SceneGlobals* g, uint32_t* hist, int nhist) {
 // Scene bounds (kernels/scene.cu:72-85) and the largest triangle extent.
 __global__ void __launch_bounds__(256) k_bounds(const float* __restrict__ V, const int* __restrict__ vidx, int n,
                                                 SceneGlobals* g) {
+  pdl_wait();
+  pdl_launch_dependents();
   float lo[3] = {1e9f, 1e9f, 1e9f}, hi[3] = {-1e9f, -1e9f, -1e9f}, e = 0.f;
   bool ok = true;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
@@ -202,12 +217,17 @@ __device__ __forceinline__ void load_scene_box(const SceneGlobals* g, float mn[3
 }
 
 // Morton codes + per-pass digit histograms; also clears the look-back status.
+// (Counting each digit once per group of lanes that share it, with
+// __match_any_sync, measured 31 us against 25 us for per-lane shared atomics
+// on the 1M-triangle build.)
 __global__ void __launch_bounds__(512, 2) k_morton(const float* __restrict__ V, const int* __restrict__ vidx, int n,
                                                 const SceneGlobals* g, uint32_t* __restrict__ keys,
                                                 uint32_t* __restrict__ hist, int passes,
                                                 uint32_t* __restrict__ status, int status_words) {
   __shared__ uint32_t sh[3 * kRadix];
   for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) sh[i] = 0;
+  pdl_wait();
+  pdl_launch_dependents();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < status_words; i += gridDim.x * blockDim.x) status[i] = 0;
   float mn[3], mx[3];
   load_scene_box(g, mn, mx);
@@ -352,8 +372,10 @@ __global__ void __launch_bounds__(TH) k_onesweep(const uint32_t* __restrict__ ki
   __shared__ uint32_t s_warp[W];
   __shared__ int s_tile;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) s_tile = (int)atomicAdd(tile_counter, 1u);
   for (int i = tid; i < W * kRadix / 2; i += TH) (&s_whist[0][0])[i] = 0;
+  pdl_wait();
+  pdl_launch_dependents();
+  if (tid == 0) s_tile = (int)atomicAdd(tile_counter, 1u);
   // global start of each digit: exclusive scan of the pass histogram
   uint32_t gh[DPT], gsum = 0;
 #pragma unroll
@@ -522,47 +544,69 @@ __device__ __forceinline__ int warp_prefix_end(int limit, Pred pred) {
 // BuildHierarchy (kernels/bvh.cu:164-207) with FindSpan (bvh.cu:100-133) and
 // FindSplit (bvh.cu:134-162): one thread per internal node writes its
 // children's parent words and clears the node's refit flag (the child codes
-// reach the wide nodes through the refit, with the boxes).  A node whose
-// span turns out longer than kShortSpan leaves (the nodes near the root,
-// whose binary searches are the longest chains of dependent loads) is
-// searched by its whole warp, 32 candidates at a time.  (Measured neutral
-// on the 1M-triangle build: the kernel's time is the short searches' L2
-// latency over its 3.2 waves, not the near-root chains.)  Both searches look
-// for the end of a prefix on which the reference's predicate holds (common
-// prefix with the node's first key longer than at the span's other end), so
-// they return the reference's span and split.
+// and boxes reach the wide nodes through the refit, which relies on the
+// empty odd slot marked here beside a leaf child).  Every probe of a node
+// whose span is at most kShortSpan leaves lies within kShortSpan of the node,
+// so a block first stages the codes of its nodes +- kShortSpan in shared
+// memory (one coalesced load) and searches there.  A node whose span turns
+// out longer (the nodes near the root, whose binary searches are the longest
+// chains of dependent loads) is searched by its whole warp in global memory,
+// 32 candidates at a time.  Both searches look for the end of a prefix on
+// which the reference's predicate holds (common prefix with the node's first
+// key longer than at the span's other end), so they return the reference's
+// span and split.
 constexpr int kShortSpan = 512;
-__global__ void __launch_bounds__(256) k_hierarchy(const uint32_t* __restrict__ codes, int n,
-                                                   uint32_t* __restrict__ parent, int* __restrict__ flags,
-                                                   WNode* __restrict__ wnodes) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+constexpr int kHierThreads = 256;
+constexpr int kHierWindow = kHierThreads + 2 * kShortSpan + 1;
+
+// delta() on the shared-memory window (j within it, or out of [0, n): -1).
+__device__ __forceinline__ int kdelta_s(const uint32_t* s_c, int w0, int n, uint64_t ki, int j) {
+  if (j < 0 || j >= n) return -1;
+  const uint64_t kj = ((uint64_t)s_c[j - w0] << 32) | (uint32_t)j;
+  return __clzll((long long)(ki ^ kj));
+}
+
+__global__ void __launch_bounds__(kHierThreads) k_hierarchy(const uint32_t* __restrict__ codes, int n,
+                                                            uint32_t* __restrict__ parent, int* __restrict__ flags,
+                                                            WNode* __restrict__ wnodes) {
+  __shared__ uint32_t s_c[kHierWindow];
+  pdl_wait();
+  pdl_launch_dependents();
+  const int i0 = blockIdx.x * kHierThreads;
+  const int w0 = i0 - kShortSpan;
+  for (int j = threadIdx.x; j < kHierWindow; j += kHierThreads) {
+    const int g = w0 + j;
+    s_c[j] = (g >= 0 && g < n) ? __ldg(codes + g) : 0u;
+  }
+  __syncthreads();
+  const int i = i0 + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const bool act = i < n - 1;
   int d = 1, dmin = 0, lo = 0, hi = 0, split = 0;
   bool wide = false;
   if (act) {
-    const uint64_t ki = ((uint64_t)__ldg(codes + i) << 32) | (uint32_t)i;
-    const int dd = kdelta(codes, n, ki, i + 1) - kdelta(codes, n, ki, i - 1);
+    const uint64_t ki = ((uint64_t)s_c[i - w0] << 32) | (uint32_t)i;
+    const int dd = kdelta_s(s_c, w0, n, ki, i + 1) - kdelta_s(s_c, w0, n, ki, i - 1);
     d = dd > 0 ? 1 : (dd < 0 ? -1 : 0);
-    dmin = kdelta(codes, n, ki, i - d);
+    dmin = kdelta_s(s_c, w0, n, ki, i - d);
     int lmax = 2;
-    while (lmax <= kShortSpan && kdelta(codes, n, ki, i + lmax * d) > dmin) lmax *= 2;
+    while (lmax <= kShortSpan && kdelta_s(s_c, w0, n, ki, i + lmax * d) > dmin) lmax *= 2;
     wide = lmax > kShortSpan;
     if (!wide) {
       int l = 0, t = lmax;
       do {
         t /= 2;
-        if (kdelta(codes, n, ki, i + (l + t) * d) > dmin) l += t;
+        if (kdelta_s(s_c, w0, n, ki, i + (l + t) * d) > dmin) l += t;
       } while (t > 1);
       lo = min(i, i + l * d), hi = max(i, i + l * d);
       int left = lo, right = hi;
-      uint64_t kl = ((uint64_t)__ldg(codes + left) << 32) | (uint32_t)left;
-      const int same = kdelta(codes, n, kl, right);
+      uint64_t kl = ((uint64_t)s_c[left - w0] << 32) | (uint32_t)left;
+      const int same = kdelta_s(s_c, w0, n, kl, right);
       do {
         const int s = (right + left) / 2;
-        if (kdelta(codes, n, kl, s) > same) {
+        if (kdelta_s(s_c, w0, n, kl, s) > same) {
           left = s;
-          kl = ((uint64_t)__ldg(codes + left) << 32) | (uint32_t)left;
+          kl = ((uint64_t)s_c[left - w0] << 32) | (uint32_t)left;
         } else {
           right = s;
         }
@@ -650,6 +694,8 @@ __device__ __forceinline__ void sibling_box(const WNode* W, int gp, bool p_left,
 __global__ void __launch_bounds__(256) k_refit_top(WNode* wnodes, const uint32_t* __restrict__ parent,
                                                    const uint32_t* __restrict__ arrivals, int n, int* flags,
                                                    SceneGlobals* g) {
+  pdl_wait();
+  pdl_launch_dependents();
   const unsigned count = *(volatile unsigned*)&g->narr;
   for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
     uint32_t w = __ldg(arrivals + i);
@@ -711,6 +757,8 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__
   __shared__ float4 s_box[kRefitBlock][2][2];  // children's boxes at each block-local node (lo, hi)
   __shared__ int s_flag[kRefitBlock];
   s_flag[threadIdx.x] = 0;
+  pdl_wait();
+  pdl_launch_dependents();
   __syncthreads();
   const int k0 = blockIdx.x * kRefitBlock;
   const int k = k0 + threadIdx.x;
@@ -973,6 +1021,8 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit_batch(const float* __rest
   __shared__ float4 s_box[kRefitBlock][2][2];
   __shared__ int s_flag[kRefitBlock];
   s_flag[threadIdx.x] = 0;
+  pdl_wait();
+  pdl_launch_dependents();
   __syncthreads();
   const int k0 = blockIdx.x * kRefitBlock;
   const int k = k0 + threadIdx.x;
@@ -1108,13 +1158,6 @@ namespace {
 __global__ void k_refit_init(SceneGlobals* g) {
   if (threadIdx.x == 0) g->emax = f2ord(0.f), g->narr = 0u;
 }
-
-void refit(const MeshBufs& m, const BuildBufs& b, cudaStream_t st) {
-  const int n = m.ntri;
-  k_refit<<<(n + kRefitBlock - 1) / kRefitBlock, kRefitBlock, 0, st>>>(m.verts, m.vidx, b.vals_b, n, b.wnodes,
-                                                                        b.leaves, b.parent, b.arrivals, b.g);
-  if (n > kRefitBlock) k_refit_top<<<num_sms() * 2, 256, 0, st>>>(b.wnodes, b.parent, b.arrivals, n, b.flags, b.g);
-}
 }  // namespace
 
 int num_sms() {
@@ -1128,16 +1171,51 @@ int num_sms() {
   return sms;
 }
 
+// Launches kernel k on st with `grid` blocks of `block` threads, as a
+// programmatic dependent of the kernel launched on st before it (dep) or the
+// ordinary way.
+template <typename... P, typename... A>
+static void launch_k(bool dep, void (*k)(P...), int grid, int block, cudaStream_t st, A... args) {
+  if (!dep) {
+    k<<<grid, block, 0, st>>>(args...);
+    return;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // One sort pass in the shape sort_large(n) picks; `status` holds the
 // pass's sort_tiles(n) * kRadix words (enough for either shape).
 static void onesweep_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, int n, int shift,
-                          const uint32_t* ghist, uint32_t* status, unsigned* counter, int* err, cudaStream_t st) {
+                          const uint32_t* ghist, uint32_t* status, unsigned* counter, int* err, cudaStream_t st,
+                          bool dep = false) {
   if (sort_large(n))
-    k_onesweep<kSortThreadsL, kSortItems><<<sort_tiles_used(n), kSortThreadsL, 0, st>>>(kin, vin, kout, vout, n, shift,
-                                                                                        ghist, status, counter, err);
+    launch_k(dep, k_onesweep<kSortThreadsL, kSortItems>, sort_tiles_used(n), kSortThreadsL, st, kin, vin, kout, vout,
+             n, shift, ghist, status, counter, err);
   else
-    k_onesweep<kSortThreads, kSortItems><<<sort_tiles_used(n), kSortThreads, 0, st>>>(kin, vin, kout, vout, n, shift,
-                                                                                      ghist, status, counter, err);
+    launch_k(dep, k_onesweep<kSortThreads, kSortItems>, sort_tiles_used(n), kSortThreads, st, kin, vin, kout, vout, n,
+             shift, ghist, status, counter, err);
+}
+
+// The refit and its spanning-node pass, as programmatic dependents of the
+// kernel before them.
+static void refit(const MeshBufs& m, const BuildBufs& b, cudaStream_t st) {
+  const int n = m.ntri;
+  launch_k(true, k_refit, (n + kRefitBlock - 1) / kRefitBlock, kRefitBlock, st, (const float*)m.verts,
+           (const int*)m.vidx, (const uint32_t*)b.vals_b, n, b.wnodes, b.leaves, (const uint32_t*)b.parent,
+           b.arrivals, b.g);
+  if (n > kRefitBlock)
+    launch_k(true, k_refit_top, num_sms() * 2, 256, st, b.wnodes, (const uint32_t*)b.parent,
+             (const uint32_t*)b.arrivals, n, b.flags, b.g);
 }
 
 cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st) {
@@ -1148,9 +1226,10 @@ cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st)
   k_build_init<<<1, 1024, 0, st>>>(b.g, b.hist, passes * kRadix);
   const int sms = num_sms();
   const int gb = min((n + 255) / 256, sms * 8);
-  k_bounds<<<gb, 256, 0, st>>>(m.verts, m.vidx, n, b.g);
+  launch_k(true, k_bounds, gb, 256, st, (const float*)m.verts, (const int*)m.vidx, n, b.g);
   const int gm = min((n + 511) / 512, sms * 2);
-  k_morton<<<gm, 512, 0, st>>>(m.verts, m.vidx, n, b.g, b.keys_a, b.hist, passes, b.status, passes * tiles * kRadix);
+  launch_k(true, k_morton, gm, 512, st, (const float*)m.verts, (const int*)m.vidx, n, (const SceneGlobals*)b.g,
+           b.keys_a, b.hist, passes, b.status, passes * tiles * kRadix);
   // pass 0: keys_a -> keys_b (values 0..n-1), pass 1: b -> a, pass 2: a -> b
   const uint32_t* kin = b.keys_a;
   const uint32_t* vin = nullptr;
@@ -1158,11 +1237,13 @@ cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st)
     uint32_t* ko = (p & 1) ? b.keys_a : b.keys_b;
     uint32_t* vo = (p & 1) ? b.vals_a : b.vals_b;
     onesweep_pass(kin, vin, ko, vo, n, p * kRadixBits, b.hist + p * kRadix, b.status + (size_t)p * tiles * kRadix,
-                  &b.g->tile_counter[p], &b.g->err, st);
+                  &b.g->tile_counter[p], &b.g->err, st, true);
     kin = ko;
     vin = vo;
   }
-  if (n >= 2) k_hierarchy<<<(n - 1 + 255) / 256, 256, 0, st>>>(b.keys_b, n, b.parent, b.flags, b.wnodes);
+  if (n >= 2)
+    launch_k(true, k_hierarchy, (n - 1 + kHierThreads - 1) / kHierThreads, kHierThreads, st,
+             (const uint32_t*)b.keys_b, n, b.parent, b.flags, b.wnodes);
   refit(m, b, st);
   return cudaGetLastError();
 }
@@ -1233,7 +1314,8 @@ __global__ void __launch_bounds__(256) k_nodes3(const uint32_t* __restrict__ par
 cudaError_t launch_stage_hierarchy(const uint32_t* codes, const uint32_t* ids, int n, int* nodes3,
                                    uint32_t* parent, int* flags, WNode* wnodes, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  if (n >= 2) k_hierarchy<<<(n - 1 + 255) / 256, 256, 0, st>>>(codes, n, parent, flags, wnodes);
+  if (n >= 2)
+    k_hierarchy<<<(n - 1 + kHierThreads - 1) / kHierThreads, kHierThreads, 0, st>>>(codes, n, parent, flags, wnodes);
   k_nodes3<<<(2 * n - 1 + 255) / 256, 256, 0, st>>>(parent, ids, n, nodes3);
   return cudaGetLastError();
 }
