@@ -313,8 +313,9 @@ def run_refit_vs_rebuild(frames=60, W2=1280, H2=720, spp=4):
 def run_batched(count=256, reps=3):
     """The batched workload: 256 meshes (log-uniform 1k..500k triangles),
     each with its own camera and light, 256x256 at 4 spp.  Batched = one
-    graph replay of the segmented build + the persistent multi-scene render,
-    after the autotuner chose the launch shape; plain = the 256 meshes built
+    graph replay of the persistent launch(es) that build and render every
+    mesh (one launch, or the render in a second one: the autotuner chose the
+    faster, and the other form is timed beside it); plain = the 256 meshes built
     and rendered one after another with the plain entry points (scenes
     resident on the device).  Both timed with CUDA events, L2 flushed first;
     the images of both must be identical."""
@@ -350,6 +351,15 @@ def run_batched(count=256, reps=3):
         return float(np.median(ts))
 
     t_batch = timed(lambda: b.run(img_b, graph=True, stream=stream))
+    # the other launch form with the same shape (one launch: build and render
+    # in one persistent kernel; two: the render in its own launch)
+    other = 3 - tune["launches"]
+    b.set_tuning(tune["block_size"], tune["lanes_per_pixel"], tune["stack"], other)
+    img_o = torch.empty_like(img_b)
+    b.run(img_o, graph=True, stream=stream)
+    t_other = timed(lambda: b.run(img_o, graph=True, stream=stream))
+    same_forms = bool(torch.equal(img_o, img_b))
+    b.set_tuning(tune["block_size"], tune["lanes_per_pixel"], tune["stack"], tune["launches"])
     scenes = [crt.Scene(s.mesh) for s in scs]
     img_p = torch.empty((total_px, 3), dtype=torch.uint8, device="cuda")
     outs = [{"rgb8": img_p[b.offsets[m]:b.offsets[m + 1]]} for m in range(count)]
@@ -370,8 +380,9 @@ def run_batched(count=256, reps=3):
     return {"meshes": count, "triangles": tris, "rays": rays, "image": "256x256x4spp per mesh",
             "batched_ms": round(t_batch, 3), "plain_ms": round(t_plain, 3),
             "batched_mrays_s": round(rays / t_batch / 1e3, 1), "plain_mrays_s": round(rays / t_plain / 1e3, 1),
-            "speedup": round(t_plain / t_batch, 3), "tuning": tune, "images_identical": same,
-            "plain_launches": 9 * count, "batched_launches": 12}
+            "speedup": round(t_plain / t_batch, 3), "tuning": tune, "images_identical": same and same_forms,
+            "plain_launches": 9 * count, "batched_launches": tune["launches"],
+            f"{other}_launch_form_ms": round(t_other, 3)}
 
 
 def run_adjoint(reps=5):

@@ -71,7 +71,7 @@ class _BatchView(C.Structure):
 
 class _BatchTuning(C.Structure):
     _fields_ = [("block_size", C.c_int32), ("lanes_per_pixel", C.c_int32), ("stack", C.c_int32),
-                ("render_ms", C.c_float)]
+                ("render_ms", C.c_float), ("launches", C.c_int32)]
 
 
 _lib = None
@@ -416,15 +416,17 @@ class Batch:
         """Split run()'s concatenated output into per-mesh (W*H, 3) views."""
         return [out[self.offsets[m]:self.offsets[m + 1]] for m in range(self.M)]
 
-    def set_tuning(self, block_size, lanes_per_pixel, stack):
-        t = _BatchTuning(block_size, lanes_per_pixel, stack, 0.0)
+    def set_tuning(self, block_size, lanes_per_pixel, stack, launches=2):
+        """launches = 1: build and render in one persistent launch; 2: the
+        render in a launch of its own."""
+        t = _BatchTuning(block_size, lanes_per_pixel, stack, 0.0, launches)
         _check(lib().crt_batch_set_tuning(self.h, C.byref(t)))
 
     def autotune(self, stream=None):
         t = _BatchTuning()
         _check(lib().crt_batch_autotune(self.h, C.byref(t), _stream(stream)))
         return dict(block_size=t.block_size, lanes_per_pixel=t.lanes_per_pixel, stack=t.stack,
-                    render_ms=float(t.render_ms))
+                    launches=t.launches, render_ms=float(t.render_ms))
 
     def check(self, stream=None):
         _check(lib().crt_batch_check(self.h, _stream(stream)))

@@ -1,17 +1,16 @@
 // batch.cu -- the batched form: many meshes, each with its own camera and
-// light, built and rendered together.  The build runs as one sequence of
-// segmented kernels over all meshes (build.cu, "batched"); the render is one
-// persistent launch whose warps claim (mesh, pixel tile) work items.  The
-// whole sequence is captured once into a CUDA graph and replayed.  The block
-// size, the warp's pixel tile and the shared-memory part of the traversal
-// stack are chosen by crt_batch_autotune.
+// light, built and rendered together by the persistent kernels of
+// batch_kernel.cuh (one launch, or the render in a second one), captured once
+// into a CUDA graph and replayed.  The block size, the lanes each pixel
+// takes, the shared-memory part of the traversal stack and the number of
+// launches are chosen by crt_batch_autotune.
 #include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
 
 #include "crt.h"
-#include "crt_internal.h"
+#include "batch_kernel.cuh"
 
 namespace crt {
 void set_last_error(const char* msg);
@@ -32,6 +31,7 @@ struct crt_batch {
   size_t image_bytes = 0;
   RenderArgs* args = nullptr;
   BatchTuning tuning;
+  unsigned* bar = nullptr;     // the grid barrier of the persistent kernel (2 words)
   cudaStream_t cap = nullptr;  // capture stream (the legacy stream cannot be captured)
   cudaGraphExec_t graph = nullptr;
 };
@@ -83,11 +83,97 @@ BatchView view_for(const crt_batch* b, const BatchTuning& t) {
   return v;
 }
 
-cudaError_t enqueue(crt_batch* b, cudaStream_t st) {
-  cudaError_t e = launch_build_batch(b->b, st);
+// One launch of k_batch<TH, SHORT> over phases [first, last]: as many
+// blocks as can be resident at once (the launch is cooperative, so the grid
+// barrier between phases cannot wait on a block that is not running).
+template <int TH, int SHORT>
+cudaError_t launch_batch_kernel(const BatchLaunch& L, cudaStream_t st) {
+  const size_t smem = batch_smem_bytes<TH>(SHORT, L.first < kPhRender);
+  void (*k)(const BatchBufs, const BatchView, int, int, unsigned*, int, int) = k_batch<TH, SHORT>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  return launch_render_batch(view_for(b, b->tuning), b->tuning, st);
+  int bps = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, TH, smem);
+  if (e != cudaSuccess) return e;
+  if (bps <= 0) return cudaErrorInvalidConfiguration;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(num_sms() * bps));
+  cfg.blockDim = dim3(TH);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, L.b, L.v, L.gmax, L.sort_tiles, L.bar, L.first, L.last);
 }
+
+// The render phase alone, in k_batch_render (persistent, not cooperative:
+// it has no grid barrier).
+template <int TH, int SHORT>
+cudaError_t launch_render_kernel(const BatchLaunch& L, cudaStream_t st) {
+  const size_t smem = batch_smem_bytes<TH>(SHORT, false);
+  void (*k)(const BatchView, int) = k_batch_render<TH, SHORT>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int bps = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, TH, smem);
+  if (e != cudaSuccess) return e;
+  k<<<num_sms() * (bps > 0 ? bps : 1), TH, smem, st>>>(L.v, L.gmax);
+  return cudaGetLastError();
+}
+
+template <int TH, int SHORT>
+cudaError_t launch_phases(const BatchLaunch& L, bool render_kernel, cudaStream_t st) {
+  return render_kernel ? launch_render_kernel<TH, SHORT>(L, st) : launch_batch_kernel<TH, SHORT>(L, st);
+}
+
+template <int TH>
+cudaError_t launch_batch_stack(const BatchLaunch& L, int stack, bool render_kernel, cudaStream_t st) {
+  switch (stack) {
+    case 8:
+      return launch_phases<TH, 8>(L, render_kernel, st);
+    case 16:
+      return launch_phases<TH, 16>(L, render_kernel, st);
+    default:
+      return launch_phases<TH, 0>(L, render_kernel, st);
+  }
+}
+
+// Enqueue phases [first, last] with tuning t.  With t.launches == 2 the
+// render phase runs in k_batch_render after k_batch has run the others.
+// The barrier words are cleared before each k_batch launch, and the render's
+// item counter before a render that the init phase of the same launch does
+// not precede.
+cudaError_t enqueue_phases(crt_batch* b, const BatchTuning& t, int first, int last, cudaStream_t st) {
+  BatchLaunch L;
+  L.b = b->b;
+  L.v = view_for(b, t);
+  L.gmax = t.lanes;
+  L.sort_tiles = sort_tiles(b->N);
+  L.bar = b->bar;
+  auto run = [&](int f, int l, bool render_kernel) -> cudaError_t {
+    L.first = f, L.last = l;
+    cudaError_t e = cudaSuccess;
+    if (!render_kernel) e = cudaMemsetAsync(b->bar, 0, 2 * sizeof(unsigned), st);
+    if (e == cudaSuccess && l == kPhRender && (f > kPhInit || render_kernel))
+      e = cudaMemsetAsync(b->v.counter, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    return t.block == 128 ? launch_batch_stack<128>(L, t.stack, render_kernel, st)
+                          : launch_batch_stack<256>(L, t.stack, render_kernel, st);
+  };
+  if (t.launches == 2 && last == kPhRender) {
+    if (first < kPhRender) {
+      const cudaError_t e = run(first, kPhRefitTop, false);
+      if (e != cudaSuccess) return e;
+    }
+    return run(kPhRender, kPhRender, true);
+  }
+  return run(first, last, false);
+}
+
+cudaError_t enqueue(crt_batch* b, cudaStream_t st) { return enqueue_phases(b, b->tuning, kPhInit, kPhRender, st); }
 
 void drop_graph(crt_batch* b) {
   if (b->graph) cudaGraphExecDestroy(b->graph);
@@ -188,7 +274,7 @@ crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* v
                        sizeof(DMat) * (size_t)Mat, 4 * (size_t)N, 4 * (size_t)(M + 1), 4 * (size_t)kLaneOptions * (M + 1),
                        5 * 4 * (size_t)N, 4 * 4 * (size_t)kRadix, 4 * 4 * (size_t)tiles * kRadix,
                        4 * (size_t)(NI + N), 4 * (size_t)(NI > 0 ? NI : 1), 0,
-                       sizeof(LeafTri) * (size_t)N, sizeof(SceneGlobals) * (size_t)M, 64, b->image_bytes,
+                       sizeof(LeafTri) * (size_t)N, sizeof(SceneGlobals) * (size_t)M, 128, b->image_bytes,
                        sizeof(RenderArgs) * (size_t)M, sizeof(WNode) * (size_t)(NI + M), sizeof(uint2) * (size_t)N};
   const int K = sizeof(sz) / sizeof(sz[0]);
   std::vector<size_t> off(K);
@@ -224,6 +310,7 @@ crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* v
   bb.g = (SceneGlobals*)at(16);
   bb.counters = (unsigned*)at(17);
   bb.err = (int*)(at(17) + 32);
+  b->bar = (unsigned*)(at(17) + 64);
   b->image = (uint8_t*)at(18);
   b->args = (RenderArgs*)at(19);
   bb.wnodes = (WNode*)at(20);
@@ -274,6 +361,7 @@ crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* v
       (e = up(d_ioff, b->item_off.data(), 4 * b->item_off.size())) != cudaSuccess ||
       (e = up(b->args, ha.data(), sizeof(RenderArgs) * M)) != cudaSuccess ||
       (e = cudaMemsetAsync(bb.flags, 0, sz[13], st)) != cudaSuccess ||
+      (e = cudaMemsetAsync(at(17), 0, sz[17], st)) != cudaSuccess ||
       (e = cudaStreamSynchronize(st)) != cudaSuccess ||
       (e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking)) != cudaSuccess) {
     cudaFree(b->block);
@@ -298,10 +386,11 @@ crt_status crt_batch_set_tuning(crt_batch* b, const crt_batch_tuning* t) {
   if (!b || !t) return fail(CRT_INVALID_ARG, "null argument");
   bool lanes_ok = false;
   for (int s = 0; s < kLaneOptions; s++) lanes_ok = lanes_ok || t->lanes_per_pixel == kLanes[s];
-  const bool ok = (t->block_size == 64 || t->block_size == 128 || t->block_size == 256) && lanes_ok &&
-                  (t->stack == 0 || t->stack == 8 || t->stack == 16);
+  const bool ok = (t->block_size == 128 || t->block_size == 256) && lanes_ok &&
+                  (t->stack == 0 || t->stack == 8 || t->stack == 16) && (t->launches == 1 || t->launches == 2);
   if (!ok) return fail(CRT_INVALID_ARG, "unsupported tuning");
   b->tuning.block = t->block_size, b->tuning.lanes = t->lanes_per_pixel, b->tuning.stack = t->stack;
+  b->tuning.launches = t->launches;
   drop_graph(b);
   return CRT_OK;
 }
@@ -344,39 +433,41 @@ crt_status crt_batch_check(crt_batch* b, void* stream) {
   return CRT_OK;
 }
 
-// Times the supported tunings on the batch (build once, then one render per
-// tuning after a warm-up render; lanes options that give every mesh the same
-// lanes per pixel as a smaller option are skipped) and keeps the fastest.
+// Times the supported tunings on the batch (build once, then the render
+// phase alone per tuning after a warm-up render, in k_batch for the
+// one-launch form and in k_batch_render for the two-launch form; lanes
+// options that give every mesh the same lanes per pixel as a smaller option
+// are skipped) and keeps the fastest.
 crt_status crt_batch_autotune(crt_batch* b, crt_batch_tuning* chosen, void* stream) {
   if (!b) return fail(CRT_INVALID_ARG, "null batch");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const int blocks[] = {64, 128, 256};
+  const int blocks[] = {128, 256};
   const int stacks[] = {0, 8, 16};
   cudaEvent_t e0, e1;
   CRT_CUDA(cudaEventCreate(&e0), "event");
   CRT_CUDA(cudaEventCreate(&e1), "event");
   BatchTuning best = b->tuning;
   float best_ms = 1e30f;
-  CRT_CUDA(launch_build_batch(b->b, st), "build");
-  CRT_CUDA(launch_render_batch(view_for(b, best), best, st), "render");  // warm-up
+  CRT_CUDA(enqueue_phases(b, best, kPhInit, kPhRefitTop, st), "build");
+  CRT_CUDA(enqueue_phases(b, best, kPhRender, kPhRender, st), "render");  // warm-up
   for (int li = 0; li < kLaneOptions; li++) {
     bool same = li > 0;
     for (int m = 0; m < b->M && same; m++)
       same = lanes_per_pixel(b->views[m].spp, kLanes[li]) == lanes_per_pixel(b->views[m].spp, kLanes[li - 1]);
     if (same) continue;
     for (int bs : blocks)
-      for (int sk : stacks) {
-        BatchTuning t;
-        t.block = bs, t.lanes = kLanes[li], t.stack = sk;
-        const BatchView v = view_for(b, t);
-        CRT_CUDA(cudaEventRecord(e0, st), "event");
-        CRT_CUDA(launch_render_batch(v, t, st), "render");
-        CRT_CUDA(cudaEventRecord(e1, st), "event");
-        CRT_CUDA(cudaEventSynchronize(e1), "event");
-        float ms = 0.f;
-        CRT_CUDA(cudaEventElapsedTime(&ms, e0, e1), "event");
-        if (ms < best_ms) best_ms = ms, best = t;
-      }
+      for (int sk : stacks)
+        for (int nl = 1; nl <= 2; nl++) {
+          BatchTuning t;
+          t.block = bs, t.lanes = kLanes[li], t.stack = sk, t.launches = nl;
+          CRT_CUDA(cudaEventRecord(e0, st), "event");
+          CRT_CUDA(enqueue_phases(b, t, kPhRender, kPhRender, st), "render");
+          CRT_CUDA(cudaEventRecord(e1, st), "event");
+          CRT_CUDA(cudaEventSynchronize(e1), "event");
+          float ms = 0.f;
+          CRT_CUDA(cudaEventElapsedTime(&ms, e0, e1), "event");
+          if (ms < best_ms) best_ms = ms, best = t;
+        }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -384,6 +475,7 @@ crt_status crt_batch_autotune(crt_batch* b, crt_batch_tuning* chosen, void* stre
   drop_graph(b);
   if (chosen) {
     chosen->block_size = best.block, chosen->lanes_per_pixel = best.lanes, chosen->stack = best.stack;
+    chosen->launches = best.launches;
     chosen->render_ms = best_ms;
   }
   return CRT_OK;

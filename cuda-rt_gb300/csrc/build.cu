@@ -13,47 +13,11 @@
 // from the three vertices (L2-resident for the sizes this targets).
 #include <cstdio>
 
-#include "crt_internal.h"
+#include "build_device.cuh"
 
 namespace crt {
 
 namespace {
-
-constexpr int kSpinLimit = 1 << 20;  // bounded look-back wait (x ~64 ns)
-
-// Programmatic dependent launch.  The plain build launches its kernels as
-// programmatic dependents of the kernel before them (launch_dep): a
-// dependent's blocks may be scheduled once every block of the kernel before
-// it has started, and pdl_wait() holds them until that kernel has completed
-// and its writes are visible.  Every build kernel calls pdl_wait() before it
-// touches global memory and then lets its own dependents be scheduled, so a
-// stage boundary no longer costs a launch.  Launched the ordinary way, both
-// instructions are no-ops.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
-
-__device__ __forceinline__ void tri_box(const float* __restrict__ V, const int* __restrict__ vidx, int t,
-                                        float3& a, float3& b, float3& c, float lo[3], float hi[3]) {
-  const int ia = __ldg(vidx + 3 * t), ib = __ldg(vidx + 3 * t + 1), ic = __ldg(vidx + 3 * t + 2);
-  a = make_float3(__ldg(V + 3 * ia), __ldg(V + 3 * ia + 1), __ldg(V + 3 * ia + 2));
-  b = make_float3(__ldg(V + 3 * ib), __ldg(V + 3 * ib + 1), __ldg(V + 3 * ib + 2));
-  c = make_float3(__ldg(V + 3 * ic), __ldg(V + 3 * ic + 1), __ldg(V + 3 * ic + 2));
-  // computeTriangleBoundingBox (kernels/scene.cu:120-130) through
-  // minimum/maximum (fminf/fmaxf): exact on float inputs.
-  lo[0] = fminf(c.x, fminf(a.x, b.x)), hi[0] = fmaxf(c.x, fmaxf(a.x, b.x));
-  lo[1] = fminf(c.y, fminf(a.y, b.y)), hi[1] = fmaxf(c.y, fmaxf(a.y, b.y));
-  lo[2] = fminf(c.z, fminf(a.z, b.z)), hi[2] = fmaxf(c.z, fmaxf(a.z, b.z));
-}
-
-// Every coordinate finite and |x| <= 1e37 (fminf/fmaxf would hide a NaN
-// inside the box, so the vertices themselves are checked).
-__device__ __forceinline__ bool finite_coords(float3 a, float3 b, float3 c) {
-  const float m = fmaxf(fmaxf(fmaxf(fabsf(a.x), fabsf(a.y)), fmaxf(fabsf(a.z), fabsf(b.x))),
-                        fmaxf(fmaxf(fabsf(b.y), fabsf(b.z)), fmaxf(fmaxf(fabsf(c.x), fabsf(c.y)), fabsf(c.z))));
-  const bool nan = (a.x != a.x) | (a.y != a.y) | (a.z != a.z) | (b.x != b.x) | (b.y != b.y) | (b.z != b.z) |
-                   (c.x != c.x) | (c.y != c.y) | (c.z != c.z);
-  return !nan && m <= 1e37f;
-}
 
 __global__ void k_build_init(SceneGlobals* g, uint32_t* hist, int nhist) {
   pdl_wait();
@@ -125,95 +89,6 @@ __global__ void __launch_bounds__(256) k_bounds(const float* __restrict__ V, con
       atomicMax(&g->emax, f2ord(v));
   }
   if (threadIdx.x == 0 && s_bad) atomicOr(&g->err, kErrNonFinite);
-}
-
-__device__ __forceinline__ uint32_t expand_bits(uint32_t v) {  // ExpandBits, kernels/bvh.cu:13-21
-  v = (v * 0x00010001u) & 0xFF0000FFu;
-  v = (v * 0x00000101u) & 0x0F00F00Fu;
-  v = (v * 0x00000011u) & 0xC30C30C3u;
-  v = (v * 0x00000005u) & 0x49249249u;
-  return v;
-}
-
-// One axis of CalculateMortonCode (kernels/bvh.cu:25-27) on the normalised
-// centroid p: (float)min(max(p*1024, 0), 1023) with NaN-ignoring max/min,
-// truncated to unsigned.
-__device__ __forceinline__ uint32_t morton_axis(double p) {
-  double s = p * 1024.0;
-  s = fmax(s, 0.0);
-  s = fmin(s, 1023.0);
-  return (uint32_t)__double2float_rn(s);
-}
-
-// computeMortonCodesKernel, kernels/bvh.cu:37-61, in double as the reference:
-// c = 0.5*(lo+hi), q = (c-mn)/(mx-mn), cell = trunc(RN32(clamp(1024 q))).
-static __device__ __noinline__ uint32_t morton_axis_exact(float lo, float hi, double mn, double mx) {
-  double c = 0.5 * ((double)lo + (double)hi);
-  c = (c - mn) / (mx - mn);
-  return morton_axis(c);
-}
-
-// Exact sum a + b as an unevaluated pair (s, e): s = RN(a + b), e the error.
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = __fadd_rn(a, b);
-  const float bb = __fsub_rn(s, a);
-  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-
-// The same cell without double arithmetic whenever that is provably right.
-// y = 1024 (c - mn) / (mx - mn) is formed in float-float: c = (lo + hi)/2,
-// c - mn and mx - mn by exact two-sums, then one division with an FMA-based
-// correction, so y_hi + y_lo is within E = 2^-30 (|y| + 1024 (|c| + |mn|)/den)
-// of the exact quotient (about 2^10 over a first-order bound; the double path's
-// own error is smaller still).  The cell is floor(y) unless y sits within half
-// a float ulp (<= 2^-15 below 1024) of the next integer, or the bound does not
-// separate y from an integer: then the double path decides.
-__device__ __forceinline__ uint32_t morton_cell(float lo, float hi, float mn, float mx) {
-  float dh, dl;
-  two_sum(mx, -mn, dh, dl);
-  if (dh > 0.f) {
-    float sh, sl;
-    two_sum(lo, hi, sh, sl);
-    const float ch = 0.5f * sh, cl = 0.5f * sl;  // exact halving
-    float nh, nl;
-    two_sum(ch, -mn, nh, nl);
-    nl = __fadd_rn(nl, cl);
-    const float q1 = __fdiv_rn(nh, dh);
-    // r = (nh + nl) - q1 (dh + dl), with q1*dh split exactly by an FMA
-    const float ph = __fmul_rn(q1, dh);
-    const float pl = __fmaf_rn(q1, dh, -ph);
-    const float r = __fadd_rn(__fsub_rn(__fsub_rn(nh, ph), pl), __fsub_rn(nl, __fmul_rn(q1, dl)));
-    const float q2 = __fdiv_rn(r, dh);
-    const float yh = 1024.f * q1, yl = 1024.f * q2;  // exact scaling
-    const float E = __fmul_ru(9.3132257e-10f, __fadd_ru(fabsf(yh), __fmul_ru(1024.f, __fdiv_ru(__fadd_ru(fabsf(ch),
-                                                                                                   fabsf(mn)), dh))));
-    if (__fadd_ru(__fadd_ru(yh, yl), E) < 0.f) return 0u;
-    if (__fsub_rd(__fsub_rd(yh, -yl), E) > 1023.f) return 1023u;
-    const float fl = floorf(yh);
-    if (fl >= 0.f && fl <= 1023.f) {
-      const float fr = __fsub_rn(yh, fl);  // exact: fl <= yh < fl + 1
-      // need fr + yl in [E, 1 - 2^-14 - E)
-      if (__fsub_rd(__fadd_rd(fr, yl), E) >= 0.f && __fadd_ru(__fadd_ru(fr, yl), E) < 0.99993896484375f)
-        return (uint32_t)fl;
-    }
-  }
-  return morton_axis_exact(lo, hi, (double)mn, (double)mx);
-}
-
-__device__ __forceinline__ uint32_t morton_code(const float lo[3], const float hi[3], const float mn[3],
-                                                const float mx[3]) {
-  const uint32_t ex = expand_bits(morton_cell(lo[0], hi[0], mn[0], mx[0]));
-  const uint32_t ey = expand_bits(morton_cell(lo[1], hi[1], mn[1], mx[1]));
-  const uint32_t ez = expand_bits(morton_cell(lo[2], hi[2], mn[2], mx[2]));
-  return ex * 4 + ey * 2 + ez;
-}
-
-__device__ __forceinline__ void load_scene_box(const SceneGlobals* g, float mn[3], float mx[3]) {
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    mn[k] = ord2f(g->bmin[k]);
-    mx[k] = ord2f(g->bmax[k]);
-  }
 }
 
 // Morton codes + per-pass digit histograms; also clears the look-back status.
@@ -298,247 +173,6 @@ __global__ void __launch_bounds__(512) k_key_hist(const uint32_t* __restrict__ k
 
 __global__ void k_zero_u32(uint32_t* p, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = 0;
-}
-
-__device__ __forceinline__ int atomic_add_acq_rel(int* p, int v) {
-  int old;
-  asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
-  return old;
-}
-
-__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
-  uint32_t v;
-  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
-  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ uint32_t lanemask_lt() {
-  uint32_t m;
-  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-  return m;
-}
-
-// Exclusive scan over the block of one value per thread; returns the prefix.
-template <int TH>
-__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_warp, uint32_t& total) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) s_warp[warp] = x;
-  __syncthreads();
-  uint32_t wpre = 0, tot = 0;
-  for (int w = 0; w < TH / 32; w++) {
-    const uint32_t s = s_warp[w];
-    if (w < warp) wpre += s;
-    tot += s;
-  }
-  __syncthreads();
-  total = tot;
-  return wpre + x - v;
-}
-
-constexpr uint32_t kFlagAgg = 1u << 30, kFlagInc = 2u << 30, kValMask = (1u << 30) - 1;
-
-// One stable LSD pass over the digit at `shift` (thrust::sort_by_key's
-// role, kernels/bvh.cu:267-273).  Tiles of TH * IT keys are claimed in order
-// from an atomic counter; within a tile, warps rank their 32 * IT keys in
-// input order with __match_any_sync, and the tile's digit offsets come from a
-// decoupled look-back over the tiles before it.  Two shapes (sort_large):
-// 2048-key tiles of 256 threads for small inputs, 8192-key tiles of 1024
-// threads from 2^19 keys on (a quarter of the tiles, so a quarter of the
-// look-back chain; 45 us less per 1M-key build, 20 us more at 100k).
-template <int TH, int IT>
-__global__ void __launch_bounds__(TH) k_onesweep(const uint32_t* __restrict__ kin,
-                                                           const uint32_t* __restrict__ vin,
-                                                           uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
-                                                           int n, int shift, const uint32_t* __restrict__ ghist,
-                                                           uint32_t* __restrict__ status, unsigned* tile_counter,
-                                                           int* err) {
-  constexpr int W = TH / 32;
-  constexpr int TILE = TH * IT;
-  constexpr int DPT = kRadix / TH;  // digits per thread
-  static_assert(kRadix % TH == 0 && 32 * IT < 65536, "digits per thread, 16-bit warp counters");
-  __shared__ uint32_t s_whist[W][kRadix / 2];  // per-warp 16-bit digit counters
-  __shared__ uint32_t s_tstart[kRadix];
-  __shared__ uint32_t s_gbase[kRadix];
-  __shared__ uint32_t s_keys[TILE];
-  __shared__ uint32_t s_vals[TILE];
-  __shared__ uint32_t s_warp[W];
-  __shared__ int s_tile;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int i = tid; i < W * kRadix / 2; i += TH) (&s_whist[0][0])[i] = 0;
-  pdl_wait();
-  pdl_launch_dependents();
-  if (tid == 0) s_tile = (int)atomicAdd(tile_counter, 1u);
-  // global start of each digit: exclusive scan of the pass histogram
-  uint32_t gh[DPT], gsum = 0;
-#pragma unroll
-  for (int j = 0; j < DPT; j++) gh[j] = __ldg(ghist + DPT * tid + j), gsum += gh[j];
-  uint32_t gtot;
-  uint32_t gpre = block_excl_scan<TH>(gsum, s_warp, gtot);
-  const int tile = s_tile;
-  const int base = tile * TILE;
-  const uint32_t mask = kRadix - 1;
-  uint32_t key[IT], val[IT], rank[IT];
-  unsigned short* wh = reinterpret_cast<unsigned short*>(s_whist[warp]);
-  const uint32_t lt = lanemask_lt();
-#pragma unroll
-  for (int r = 0; r < IT; r++) {
-    const int idx = base + warp * (32 * IT) + r * 32 + lane;
-    const bool valid = idx < n;
-    key[r] = valid ? __ldg(kin + idx) : 0u;
-    val[r] = valid ? (vin ? __ldg(vin + idx) : (uint32_t)idx) : 0u;
-    const uint32_t d = valid ? ((key[r] >> shift) & mask) : (uint32_t)kRadix;
-    const uint32_t peers = __match_any_sync(0xffffffffu, d);
-    const int leader = __ffs(peers) - 1;
-    uint32_t b = 0;
-    if (lane == leader && valid) {
-      b = wh[d];
-      wh[d] = (unsigned short)(b + __popc(peers));
-    }
-    b = __shfl_sync(0xffffffffu, b, leader);
-    rank[r] = b + __popc(peers & lt);
-    __syncwarp();
-  }
-  __syncthreads();
-  // per digit: warp offsets (exclusive, in place) and the tile count
-  uint32_t cnt[DPT], csum = 0;
-#pragma unroll
-  for (int j = 0; j < DPT; j++) {
-    const int d = DPT * tid + j;
-    uint32_t c = 0;
-#pragma unroll
-    for (int w = 0; w < W; w++) {
-      unsigned short* h = reinterpret_cast<unsigned short*>(s_whist[w]) + d;
-      const uint32_t x = *h;
-      *h = (unsigned short)c;
-      c += x;
-    }
-    cnt[j] = c;
-    csum += c;
-  }
-  // publish this tile's counts, then look back for the prefix over earlier tiles
-  uint32_t* my = status + (size_t)tile * kRadix;
-#pragma unroll
-  for (int j = 0; j < DPT; j++) st_relaxed(my + DPT * tid + j, (tile == 0 ? kFlagInc : kFlagAgg) | cnt[j]);
-  uint32_t pre[DPT];
-#pragma unroll
-  for (int j = 0; j < DPT; j++) pre[j] = 0;
-  if (tile > 0) {
-    // The thread's DPT digits walk back together: DPT independent loads
-    // per L2 round trip.  A walk stops at the first inclusive prefix.
-    int look[DPT];
-#pragma unroll
-    for (int j = 0; j < DPT; j++) look[j] = tile - 1;
-    int spins = 0;
-    uint32_t live = (1u << DPT) - 1u;
-    while (live) {
-      uint32_t sv[DPT];
-#pragma unroll
-      for (int j = 0; j < DPT; j++)
-        sv[j] = (live >> j) & 1 ? ld_relaxed(status + (size_t)look[j] * kRadix + DPT * tid + j) : 0u;
-      bool waiting = false;
-#pragma unroll
-      for (int j = 0; j < DPT; j++) {
-        if (!((live >> j) & 1)) continue;
-        const uint32_t f = sv[j] & ~kValMask;
-        if (f == 0) {
-          waiting = true;
-          continue;
-        }
-        pre[j] += sv[j] & kValMask;
-        if (f == kFlagInc || look[j] == 0) {
-          live &= ~(1u << j);
-          st_relaxed(my + DPT * tid + j, kFlagInc | (pre[j] + cnt[j]));
-        } else {
-          look[j]--;
-        }
-      }
-      if (waiting) {
-        // bounded wait; once any wait has timed out, later ones give up at once
-        if (++spins > kSpinLimit || ((spins & 1023) == 0 && (ld_relaxed((const uint32_t*)err) & kErrTimeout))) {
-          atomicOr(err, kErrTimeout);
-#pragma unroll
-          for (int j = 0; j < DPT; j++)
-            if ((live >> j) & 1) st_relaxed(my + DPT * tid + j, kFlagInc | (pre[j] + cnt[j]));
-          break;
-        }
-        __nanosleep(32);
-      }
-    }
-  }
-  uint32_t ctot;
-  uint32_t cpre = block_excl_scan<TH>(csum, s_warp, ctot);
-  {
-    uint32_t c = cpre, g = gpre;
-#pragma unroll
-    for (int j = 0; j < DPT; j++) {
-      const int d = DPT * tid + j;
-      s_tstart[d] = c;
-      s_gbase[d] = g + pre[j] - c;
-      c += cnt[j];
-      g += gh[j];
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int r = 0; r < IT; r++) {
-    const int idx = base + warp * (32 * IT) + r * 32 + lane;
-    if (idx < n) {
-      const uint32_t d = (key[r] >> shift) & mask;
-      const uint32_t pos = s_tstart[d] + wh[d] + rank[r];
-      s_keys[pos] = key[r];
-      s_vals[pos] = val[r];
-    }
-  }
-  __syncthreads();
-  const int tile_n = min(TILE, n - base);
-  for (int i = tid; i < tile_n; i += TH) {
-    const uint32_t k = s_keys[i];
-    const uint32_t pos = s_gbase[(k >> shift) & mask] + (uint32_t)i;
-    kout[pos] = k;
-    vout[pos] = s_vals[i];
-  }
-}
-
-// delta(), kernels/bvh.cu:71-88: with the augmented key (code << 32 | index)
-// the common-prefix length is one 64-bit clz -- clz(ci ^ cj) when the codes
-// differ, 32 + clz(i ^ j) when they are equal, exactly the reference's two
-// cases; -1 out of range.
-__device__ __forceinline__ int kdelta(const uint32_t* __restrict__ c, int n, uint64_t ki, int j) {
-  if (j < 0 || j >= n) return -1;
-  const uint64_t kj = ((uint64_t)__ldg(c + j) << 32) | (uint32_t)j;
-  return __clzll((long long)(ki ^ kj));
-}
-
-// The parent word of a node: parent index | bit 31 when the node is its
-// parent's left child | bit 30 when the parent's leaf range crosses a
-// kRefitBlock boundary (the refit then meets at gpu scope).
-constexpr int kRefitBlock = 512;
-constexpr uint32_t kParentLeft = 1u << 31, kParentSpans = 1u << 30, kParentMask = (1u << 30) - 1;
-
-// The largest m in [0, limit] with pred(m), for a predicate true on a prefix
-// of [0, limit] (pred(0) holds): the warp evaluates 32 candidates per round,
-// log32 rounds instead of log2 dependent steps.  All 32 lanes call it with
-// the same arguments.
-template <typename Pred>
-__device__ __forceinline__ int warp_prefix_end(int limit, Pred pred) {
-  const int lane = threadIdx.x & 31;
-  int top = 1;
-  while ((int64_t)top * 32 < (int64_t)limit + 1) top *= 32;
-  int m = 0;
-  for (int stride = top; stride >= 1; stride /= 32) {
-    const int64_t cand = (int64_t)m + (int64_t)(lane + 1) * stride;
-    const bool ok = cand <= limit && pred((int)cand);
-    m += __popc(__ballot_sync(0xffffffffu, ok)) * stride;
-  }
-  return m;
 }
 
 // BuildHierarchy (kernels/bvh.cu:164-207) with FindSpan (bvh.cu:100-133) and
@@ -638,49 +272,6 @@ __global__ void __launch_bounds__(kHierThreads) k_hierarchy(const uint32_t* __re
   const float4 empty = make_float4(0.f, 0.f, 0.f, __int_as_float(kNoChild));
   if (c1 < 0) wnodes[i].s[1].lo_code = empty;
   if (c2 < 0) wnodes[i].s[3].lo_code = empty;
-}
-
-// RefitBounds (kernels/bvh.cu:209-258): one climber per leaf; at each node the
-// first arrival stops and the second computes the union (bboxunion,
-// bvh.cu:63-69) and climbs on.  min/max are exact, so every schedule gives the
-// reference's boxes.  Every box goes to the wide nodes (WNode): child x (code
-// xc) of binary node p fills slot 2*side(p) + side(x) of the wide node of p's
-// parent gp (for the root, the virtual node past the last internal one), and
-// a leaf child also fills its own slot of p's wide node (the hierarchy marks
-// the odd slot empty).  Codes are rewritten with the boxes, so a refit alone keeps
-// the wide nodes complete, and the children of every node can be read back
-// from its parent's wide node (the export does).
-//
-// A block owns kRefitBlock consecutive sorted leaves.  A node whose leaf
-// range lies inside that span has both children's climbers in the block, so
-// its two arrivals meet in shared memory with block-scope ordering (most
-// nodes).  A node spanning several blocks uses the global flag with
-// release/acquire at gpu scope and reads its other child's box from the wide
-// node.  Global flags count arrivals; each refit adds exactly two per
-// spanning node, so the parity of the old value tells first from second
-// without clearing between refits.  Each climb step needs one dependent load:
-// the parent word (index, side, spanning bit).
-__device__ __forceinline__ void put_wide(WNode* W, int xc, bool x_left, int p, int gp, bool p_left,
-                                         const float lo[3], const float hi[3]) {
-  const float4 a = make_float4(lo[0], lo[1], lo[2], __int_as_float(xc));
-  const float4 b = make_float4(hi[0], hi[1], hi[2], 0.f);
-  if (xc < 0) {  // (the hierarchy marked the odd slot empty)
-    WSlot* q = W[p].s + (x_left ? 0 : 2);
-    __stcg(&q[0].lo_code, a);
-    __stcg(&q[0].hi, b);
-  }
-  WSlot* q = W[gp].s + (p_left ? 0 : 2) + (x_left ? 0 : 1);
-  __stcg(&q->lo_code, a);
-  __stcg(&q->hi, b);
-}
-
-// The box of the other child of p, from the wide node of p's parent.
-__device__ __forceinline__ void sibling_box(const WNode* W, int gp, bool p_left, bool x_left, float lo[3],
-                                            float hi[3]) {
-  const WSlot* q = W[gp].s + (p_left ? 0 : 2) + (x_left ? 1 : 0);
-  const float4 a = __ldcg(&q->lo_code), b = __ldcg(&q->hi);
-  lo[0] = fminf(lo[0], a.x), lo[1] = fminf(lo[1], a.y), lo[2] = fminf(lo[2], a.z);
-  hi[0] = fmaxf(hi[0], b.x), hi[1] = fmaxf(hi[1], b.y), hi[2] = fmaxf(hi[2], b.z);
 }
 
 // The climb through the spanning nodes (leaf ranges over several blocks),
@@ -835,323 +426,6 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__
   }
 }
 
-// ---------------------------------------------------------------- batched
-// The same build for many meshes at once (concatenated arrays; mesh m owns
-// triangles [tri_off[m], tri_off[m+1]) and internal nodes [int_off[m],
-// int_off[m+1]), int_off[m] = tri_off[m] - m).  Child codes in the wide
-// nodes are local to the mesh, so each mesh's node and leaf ranges are a
-// self-contained tree for the traversal; parent words hold global internal
-// indices; mesh m's virtual wide node (its root's children) is NI + m.
-
-__global__ void k_batch_init(SceneGlobals* g, int M, uint32_t* hist, const int* __restrict__ tri_off,
-                             unsigned* counters, int* err) {
-  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
-#pragma unroll
-    for (int k = 0; k < 3; k++) g[m].bmin[k] = f2ord(1e9f), g[m].bmax[k] = f2ord(-1e9f);
-    g[m].emax = f2ord(0.f);
-    g[m].err = 0;
-  }
-  // passes 0-2: code digits (filled by k_morton_batch); pass 3: the mesh id,
-  // whose histogram is the mesh sizes
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * kRadix; i += gridDim.x * blockDim.x) {
-    const int p = i / kRadix, d = i % kRadix;
-    hist[i] = (p == 3 && d < M) ? (uint32_t)(tri_off[d + 1] - tri_off[d]) : 0u;
-  }
-  if (blockIdx.x == 0 && threadIdx.x < 4) counters[threadIdx.x] = 0;
-  if (blockIdx.x == 0 && threadIdx.x == 0) counters[6] = 0;  // refit hand-offs
-  if (blockIdx.x == 0 && threadIdx.x == 0) *err = 0;
-}
-
-// Per-mesh scene bounds and largest triangle extent; warps whose lanes share
-// a mesh (nearly all) reduce before their atomics.
-__global__ void __launch_bounds__(256) k_bounds_batch(const float* __restrict__ V, const int* __restrict__ vidx,
-                                                      const int* __restrict__ mesh_of, int N, SceneGlobals* g) {
-  const int stride = gridDim.x * blockDim.x;
-  for (int t0 = blockIdx.x * blockDim.x; t0 < N; t0 += stride) {
-    const int t = t0 + threadIdx.x;
-    float lo[3] = {1e9f, 1e9f, 1e9f}, hi[3] = {-1e9f, -1e9f, -1e9f}, e = 0.f;
-    bool ok = true;
-    int m = -1;
-    if (t < N) {
-      float3 a, b, c;
-      tri_box(V, vidx, t, a, b, c, lo, hi);
-      ok = finite_coords(a, b, c);
-      e = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
-      m = __ldg(mesh_of + t);
-    }
-    const unsigned peers = __match_any_sync(0xffffffffu, m);
-    if (peers == 0xffffffffu) {  // one mesh in the whole warp
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-          lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
-          hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
-        }
-        e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, o));
-      }
-      ok = __all_sync(0xffffffffu, ok);
-      if ((threadIdx.x & 31) != 0) m = -1;
-    }
-    if (m >= 0) {
-#pragma unroll
-      for (int k = 0; k < 3; k++) {
-        atomicMin(&g[m].bmin[k], f2ord(lo[k]));
-        atomicMax(&g[m].bmax[k], f2ord(hi[k]));
-      }
-      atomicMax(&g[m].emax, f2ord(e));
-      if (!ok) atomicOr(&g[m].err, kErrNonFinite);
-    }
-  }
-}
-
-// Morton codes against each triangle's own mesh box, a copy of the codes,
-// the digit histograms of the three code passes; clears the look-back status.
-__global__ void __launch_bounds__(512, 2) k_morton_batch(const float* __restrict__ V, const int* __restrict__ vidx,
-                                                      const int* __restrict__ mesh_of, int N,
-                                                      const SceneGlobals* __restrict__ g, uint32_t* __restrict__ keys,
-                                                      uint32_t* __restrict__ codes0, uint32_t* __restrict__ hist,
-                                                      uint32_t* __restrict__ status, int status_words) {
-  __shared__ uint32_t sh[3 * kRadix];
-  for (int i = threadIdx.x; i < 3 * kRadix; i += blockDim.x) sh[i] = 0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < status_words; i += gridDim.x * blockDim.x) status[i] = 0;
-  __syncthreads();
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x) {
-    float3 a, b, c;
-    float lo[3], hi[3], mn[3], mx[3];
-    tri_box(V, vidx, t, a, b, c, lo, hi);
-    load_scene_box(g + __ldg(mesh_of + t), mn, mx);
-    const uint32_t code = morton_code(lo, hi, mn, mx);
-    keys[t] = code;
-    codes0[t] = code;
-    for (int p = 0; p < 3; p++) atomicAdd(&sh[p * kRadix + ((code >> (p * kRadixBits)) & (kRadix - 1))], 1u);
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < 3 * kRadix; i += blockDim.x)
-    if (sh[i]) atomicAdd(&hist[i], sh[i]);
-}
-
-__global__ void k_mesh_keys(const uint32_t* __restrict__ vals, const int* __restrict__ mesh_of, int N,
-                            uint32_t* __restrict__ out) {
-  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < N; j += gridDim.x * blockDim.x)
-    out[j] = (uint32_t)__ldg(mesh_of + __ldg(vals + j));
-}
-
-__global__ void k_gather_codes(const uint32_t* __restrict__ vals, const uint32_t* __restrict__ codes0, int N,
-                               uint32_t* __restrict__ out) {
-  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < N; j += gridDim.x * blockDim.x)
-    out[j] = __ldg(codes0 + __ldg(vals + j));
-}
-
-__device__ __forceinline__ int mesh_of_internal(const int* __restrict__ tri_off, int M, int gi) {
-  // last m with int_off[m] = tri_off[m] - m <= gi
-  int lo = 0, hi = M - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (__ldg(tri_off + mid) - mid <= gi)
-      lo = mid;
-    else
-      hi = mid - 1;
-  }
-  return lo;
-}
-
-// BuildHierarchy per mesh (FindSpan/FindSplit on the mesh's sorted codes).
-__global__ void __launch_bounds__(256) k_hierarchy_batch(const uint32_t* __restrict__ codes_all,
-                                                         const int* __restrict__ tri_off, int M, int NI,
-                                                         uint32_t* __restrict__ parent,
-                                                         int* __restrict__ flags, WNode* __restrict__ wnodes) {
-  const int gi = blockIdx.x * blockDim.x + threadIdx.x;
-  if (gi >= NI) return;
-  int m = mesh_of_internal(tri_off, M, gi);
-  // meshes with one triangle own no internal node: skip to the owner
-  while (m + 1 < M && __ldg(tri_off + m + 1) - (m + 1) <= gi) m++;
-  const int t0 = __ldg(tri_off + m);
-  const int n = __ldg(tri_off + m + 1) - t0;
-  const int i = gi - (t0 - m);
-  const uint32_t* codes = codes_all + t0;
-  const uint64_t ki = ((uint64_t)__ldg(codes + i) << 32) | (uint32_t)i;
-  const int dd = kdelta(codes, n, ki, i + 1) - kdelta(codes, n, ki, i - 1);
-  const int d = dd > 0 ? 1 : (dd < 0 ? -1 : 0);
-  const int dmin = kdelta(codes, n, ki, i - d);
-  int lmax = 2;
-  while (kdelta(codes, n, ki, i + lmax * d) > dmin) lmax *= 2;
-  int l = 0, t = lmax;
-  do {
-    t /= 2;
-    if (kdelta(codes, n, ki, i + (l + t) * d) > dmin) l += t;
-  } while (t > 1);
-  const int lo = min(i, i + l * d), hi = max(i, i + l * d);
-  int left = lo, right = hi;
-  uint64_t kl = ((uint64_t)__ldg(codes + left) << 32) | (uint32_t)left;
-  const int same = kdelta(codes, n, kl, right);
-  do {
-    const int s = (right + left) / 2;
-    if (kdelta(codes, n, kl, s) > same) {
-      left = s;
-      kl = ((uint64_t)__ldg(codes + left) << 32) | (uint32_t)left;
-    } else {
-      right = s;
-    }
-  } while (right > left + 1);
-  const int split = left;
-  const int c1 = (split == lo) ? ~split : split;
-  const int c2 = (split + 1 == hi) ? ~(split + 1) : split + 1;
-  const int ib = t0 - m;  // this mesh's first internal node
-  const uint32_t spans = ((t0 + lo) / kRefitBlock != (t0 + hi) / kRefitBlock) ? kParentSpans : 0u;
-  parent[c1 < 0 ? NI + t0 + split : ib + split] = (uint32_t)gi | kParentLeft | spans;
-  parent[c2 < 0 ? NI + t0 + split + 1 : ib + split + 1] = (uint32_t)gi | spans;
-  flags[gi] = 0;
-  const float4 empty = make_float4(0.f, 0.f, 0.f, __int_as_float(kNoChild));
-  if (c1 < 0) wnodes[gi].s[1].lo_code = empty;
-  if (c2 < 0) wnodes[gi].s[3].lo_code = empty;
-}
-
-// RefitBounds per mesh; leaves at global sorted positions, the block-local /
-// spanning split as in k_refit (a node's shared slot is its first leaf's
-// global position).
-__global__ void __launch_bounds__(kRefitBlock) k_refit_batch(const float* __restrict__ V, const int* __restrict__ vidx,
-                                                             const uint32_t* __restrict__ ids,
-                                                             const int* __restrict__ mesh_of,
-                                                             const int* __restrict__ tri_off, int N, int NI,
-                                                             WNode* wnodes, LeafTri* __restrict__ leaves,
-                                                             const uint32_t* __restrict__ parent,
-                                                             uint2* __restrict__ arrivals, unsigned* narr,
-                                                             SceneGlobals* g) {
-  __shared__ float4 s_box[kRefitBlock][2][2];
-  __shared__ int s_flag[kRefitBlock];
-  s_flag[threadIdx.x] = 0;
-  pdl_wait();
-  pdl_launch_dependents();
-  __syncthreads();
-  const int k0 = blockIdx.x * kRefitBlock;
-  const int k = k0 + threadIdx.x;
-  if (k >= N) return;
-  const int tri = (int)__ldg(ids + k);
-  if ((unsigned)tri >= (unsigned)N) {  // only a corrupt sort gets here
-    atomicOr(&g[0].err, kErrStack);
-    return;
-  }
-  const int m = __ldg(mesh_of + tri);
-  const int t0 = __ldg(tri_off + m);
-  const int n = __ldg(tri_off + m + 1) - t0;
-  float3 a, b, c;
-  float lo[3], hi[3];
-  tri_box(V, vidx, tri, a, b, c, lo, hi);
-  LeafTri lt;
-  lt.v0 = make_float4(a.x, a.y, a.z, __int_as_float(tri));
-  lt.v1 = make_float4(b.x, b.y, b.z, 0.f);
-  lt.v2 = make_float4(c.x, c.y, c.z, 0.f);
-  leaves[k] = lt;
-  if (n == 1) {
-#pragma unroll
-    for (int q = 0; q < 3; q++) g[m].root_box[q] = lo[q], g[m].root_box[3 + q] = hi[q];
-    return;
-  }
-  const int root = t0 - m;
-  uint32_t w = __ldg(parent + NI + k);
-  int xc = ~(k - t0);  // codes are local to the mesh
-  for (int level = 0;; level++) {
-    const int p = (int)(w & kParentMask);
-    if (level >= kStackSize || p < root || p >= root + n - 1) {  // only a corrupt tree gets here
-      atomicOr(&g[m].err, kErrStack);
-      return;
-    }
-    const uint32_t wn = (p == root) ? 0u : __ldg(parent + p);
-    const bool is_left = (w & kParentLeft) != 0;
-    const int gp = (p == root) ? NI + m : (int)(wn & kParentMask);
-    const bool p_left = (p == root) || (wn & kParentLeft) != 0;
-    if (p != root && (gp < root || gp >= root + n - 1)) {  // only a corrupt tree gets here
-      atomicOr(&g[m].err, kErrStack);
-      return;
-    }
-    put_wide(wnodes, xc, is_left, p, gp, p_left, lo, hi);
-    if (!(w & kParentSpans)) {
-      const int sl = p + m - k0;  // global leaf position of the node's index, within this block
-      float4* mine = s_box[sl][is_left ? 0 : 1];
-      mine[0] = make_float4(lo[0], lo[1], lo[2], 0.f);
-      mine[1] = make_float4(hi[0], hi[1], hi[2], 0.f);
-      __threadfence_block();
-      if (atomicAdd(&s_flag[sl], 1) == 0) return;
-      __threadfence_block();
-      const float4* o = s_box[sl][is_left ? 1 : 0];
-      const float4 ol = o[0], oh = o[1];
-      lo[0] = fminf(lo[0], ol.x), lo[1] = fminf(lo[1], ol.y), lo[2] = fminf(lo[2], ol.z);
-      hi[0] = fmaxf(hi[0], oh.x), hi[1] = fmaxf(hi[1], oh.y), hi[2] = fmaxf(hi[2], oh.z);
-    } else {  // spanning node: the climb continues in k_refit_top_batch
-      arrivals[atomicAdd(narr, 1u)] = make_uint2(w, (uint32_t)m);
-      return;
-    }
-    if (p == root) {
-#pragma unroll
-      for (int q = 0; q < 3; q++) g[m].root_box[q] = lo[q], g[m].root_box[3 + q] = hi[q];
-      return;
-    }
-    xc = p - root;
-    w = wn;
-  }
-}
-
-// k_refit_top per mesh (the arrival carries its mesh; codes are mesh-local).
-__global__ void __launch_bounds__(256) k_refit_top_batch(WNode* wnodes, const uint32_t* __restrict__ parent,
-                                                         const uint2* __restrict__ arrivals, const unsigned* narr,
-                                                         const int* __restrict__ tri_off, int M, int NI, int* flags,
-                                                         SceneGlobals* g) {
-  const unsigned count = *(const volatile unsigned*)narr;
-  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-    const uint2 arr = __ldg(arrivals + i);
-    const int m = (int)arr.y;
-    if (m < 0 || m >= M) continue;  // only a corrupt arrival gets here
-    const int t0 = __ldg(tri_off + m), n = __ldg(tri_off + m + 1) - t0, root = t0 - m;
-    uint32_t w = arr.x;
-    int p = (int)(w & kParentMask);
-    if (p < root || p >= root + n - 1) {
-      atomicOr(&g[m].err, kErrStack);
-      continue;
-    }
-    uint32_t wn = (p == root) ? 0u : __ldg(parent + p);
-    bool is_left = (w & kParentLeft) != 0;
-    int gp = (p == root) ? NI + m : (int)(wn & kParentMask);
-    bool p_left = (p == root) || (wn & kParentLeft) != 0;
-    if (p != root && (gp < root || gp >= root + n - 1)) {
-      atomicOr(&g[m].err, kErrStack);
-      continue;
-    }
-    float lo[3], hi[3];
-    {
-      const WSlot* q = wnodes[gp].s + (p_left ? 0 : 2) + (is_left ? 0 : 1);
-      const float4 a = __ldcg(&q->lo_code), b = __ldcg(&q->hi);
-      lo[0] = a.x, lo[1] = a.y, lo[2] = a.z, hi[0] = b.x, hi[1] = b.y, hi[2] = b.z;
-    }
-    for (int level = 0;; level++) {
-      const uint32_t wn_next = (p == root) ? 0u : __ldg(parent + gp);
-      if ((atomic_add_acq_rel(flags + p, 1) & 1) == 0) break;  // first arrival
-      sibling_box(wnodes, gp, p_left, is_left, lo, hi);
-      if (p == root) {
-#pragma unroll
-        for (int q = 0; q < 3; q++) g[m].root_box[q] = lo[q], g[m].root_box[3 + q] = hi[q];
-        break;
-      }
-      const int xc = p - root;
-      w = wn;
-      p = (int)(w & kParentMask);
-      if (level >= kStackSize || p < root || p >= root + n - 1) {
-        atomicOr(&g[m].err, kErrStack);
-        break;
-      }
-      wn = wn_next;
-      is_left = (w & kParentLeft) != 0;
-      gp = (p == root) ? NI + m : (int)(wn & kParentMask);
-      p_left = (p == root) || (wn & kParentLeft) != 0;
-      if (p != root && (gp < root || gp >= root + n - 1)) {
-        atomicOr(&g[m].err, kErrStack);
-        break;
-      }
-      put_wide(wnodes, xc, is_left, p, gp, p_left, lo, hi);
-    }
-  }
-}
-
 }  // namespace
 
 namespace {
@@ -1245,46 +519,6 @@ cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st)
     launch_k(true, k_hierarchy, (n - 1 + kHierThreads - 1) / kHierThreads, kHierThreads, st,
              (const uint32_t*)b.keys_b, n, b.parent, b.flags, b.wnodes);
   refit(m, b, st);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_build_batch(const BatchBufs& b, cudaStream_t st) {
-  const int N = b.N, M = b.M;
-  if (N <= 0) return cudaSuccess;
-  const int tiles = sort_tiles(N);
-  const int sms = num_sms();
-  k_batch_init<<<(M + 255) / 256 > 4 ? (M + 255) / 256 : 4, 256, 0, st>>>(b.g, M, b.hist, b.tri_off, b.counters,
-                                                                         b.err);
-  k_bounds_batch<<<min((N + 255) / 256, sms * 8), 256, 0, st>>>(b.verts, b.vidx, b.mesh_of, N, b.g);
-  k_morton_batch<<<min((N + 511) / 512, sms * 2), 512, 0, st>>>(b.verts, b.vidx, b.mesh_of, N, b.g, b.keys_a,
-                                                                 b.codes0, b.hist, b.status,
-                                                                 4 * tiles * kRadix);
-  // code passes: a -> b -> a -> b
-  const uint32_t* kin = b.keys_a;
-  const uint32_t* vin = nullptr;
-  for (int p = 0; p < 3; p++) {
-    uint32_t* ko = (p & 1) ? b.keys_a : b.keys_b;
-    uint32_t* vo = (p & 1) ? b.vals_a : b.vals_b;
-    onesweep_pass(kin, vin, ko, vo, N, p * kRadixBits, b.hist + p * kRadix, b.status + (size_t)p * tiles * kRadix,
-                  b.counters + p, b.err, st);
-    kin = ko;
-    vin = vo;
-  }
-  // stable pass on the mesh id: ids end up grouped by mesh, by code within
-  const int ge = min((N + 255) / 256, sms * 8);
-  k_mesh_keys<<<ge, 256, 0, st>>>(b.vals_b, b.mesh_of, N, b.keys_a);
-  onesweep_pass(b.keys_a, b.vals_b, b.keys_b, b.vals_a, N, 0, b.hist + 3 * kRadix,
-                b.status + (size_t)3 * tiles * kRadix, b.counters + 3, b.err, st);
-  k_gather_codes<<<ge, 256, 0, st>>>(b.vals_a, b.codes0, N, b.keys_b);
-  if (b.NI > 0)
-    k_hierarchy_batch<<<(b.NI + 255) / 256, 256, 0, st>>>(b.keys_b, b.tri_off, M, b.NI, b.parent, b.flags,
-                                                          b.wnodes);
-  k_refit_batch<<<(N + kRefitBlock - 1) / kRefitBlock, kRefitBlock, 0, st>>>(
-      b.verts, b.vidx, b.vals_a, b.mesh_of, b.tri_off, N, b.NI, b.wnodes, b.leaves, b.parent, b.arrivals,
-      b.counters + 6, b.g);
-  if (N > kRefitBlock)
-    k_refit_top_batch<<<num_sms() * 2, 256, 0, st>>>(b.wnodes, b.parent, b.arrivals, b.counters + 6, b.tri_off, M,
-                                                      b.NI, b.flags, b.g);
   return cudaGetLastError();
 }
 

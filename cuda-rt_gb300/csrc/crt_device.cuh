@@ -422,7 +422,15 @@ __device__ __forceinline__ void cswap(float& ta, int& ca, float& tb, int& cb) {
 // round for the whole warp instead of once per lane.  A lane waits at its
 // candidate until it is tested, so the pruning bound is current when it
 // walks on.
-template <bool ANY, bool STATS = false, int SHORT = 0>
+// NC = true reads the nodes and leaf triangles through the read-only cache;
+// NC = false uses ordinary (coherent) global loads, cached in L1 as well.
+template <bool NC>
+__device__ __forceinline__ float4 ld_node(const float4* p) {
+  if (NC) return __ldg(p);
+  return __ldca(p);
+}
+
+template <bool ANY, bool STATS = false, int SHORT = 0, bool NC = true>
 __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, const float rb[6], HitRec& h, bool live,
                                         TravStats* ts = nullptr, int2* ring = nullptr) {
   bool run = live && S.ntri > 0;
@@ -467,7 +475,7 @@ __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, const fl
         const float4* np = reinterpret_cast<const float4*>(S.wnodes + node);
         float4 q[8];
 #pragma unroll
-        for (int j = 0; j < 8; j++) q[j] = __ldg(np + j);
+        for (int j = 0; j < 8; j++) q[j] = ld_node<NC>(np + j);
         int c[4];
         float t[4];
         int nhit = 0;
@@ -509,7 +517,7 @@ __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, const fl
       } else {
         if (STATS) ts->tris++;
         const float4* lp = reinterpret_cast<const float4*>(S.leaves + (~node & kLeafIndex));
-        const float4 a = __ldg(lp), b = __ldg(lp + 1), c = __ldg(lp + 2);
+        const float4 a = ld_node<NC>(lp), b = ld_node<NC>(lp + 1), c = ld_node<NC>(lp + 2);
         if (!tri_reject_sure(r, a, b, c)) {
           cand = node, pending = true;
           // the leaf's box (as the refit computes it from the same vertices)
@@ -527,7 +535,7 @@ __device__ __forceinline__ int traverse(const DScene& S, const RayC& r, const fl
     if (pending) {
       const int pos = ~cand & kLeafIndex;
       const float4* lp = reinterpret_cast<const float4*>(S.leaves + pos);
-      const float4 a = __ldg(lp), b = __ldg(lp + 1), c = __ldg(lp + 2);
+      const float4 a = ld_node<NC>(lp), b = ld_node<NC>(lp + 1), c = ld_node<NC>(lp + 2);
       bool in_box = true;
       if (~cand & kLeafBoxDue) {  // the leaf's box, as the refit computes it from the same vertices
         in_box = box_exact(r.ox, r.oy, r.oz, r.dx, r.dy, r.dz, fminf(c.x, fminf(a.x, b.x)),

@@ -49,7 +49,7 @@ struct MeshBufs {
   DMat* mats = nullptr;
 };
 
-// Many meshes in concatenated arrays (see build.cu, "batched").
+// Many meshes in concatenated arrays (see batch_kernel.cuh).
 struct BatchBufs {
   int M = 0, N = 0, NI = 0;  // meshes, triangles, internal nodes (N - M)
   const float* verts = nullptr;
@@ -64,13 +64,12 @@ struct BatchBufs {
   WNode* wnodes = nullptr;     // NI + M (codes local to each mesh; NI + m: mesh m's virtual node)
   LeafTri* leaves = nullptr;   // N
   SceneGlobals* g = nullptr;   // M
-  unsigned* counters = nullptr;  // [0..3] sort tiles, [4] render items, [6] refit hand-offs
+  unsigned* counters = nullptr;  // [0..3] sort tiles, [4] render items, [6] refit hand-offs (8 words)
   uint2* arrivals = nullptr;     // N: climbs handed from the refit to its spanning-node pass
   int* err = nullptr;
 };
 
 int num_sms();
-cudaError_t launch_build_batch(const BatchBufs& b, cudaStream_t st);
 
 // build.cu
 cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st);
@@ -178,9 +177,9 @@ struct BatchView {
   unsigned* counter = nullptr;
 };
 struct BatchTuning {
-  int block = 128, lanes = kDefaultLanesPerPixel, stack = 0;  // lanes: the most lanes a pixel may take
+  int block = 256, lanes = kDefaultLanesPerPixel, stack = 0;  // lanes: the most lanes a pixel may take
+  int launches = 2;  // 1: build and render in one launch; 2: the render in a launch of its own
 };
-cudaError_t launch_render_batch(const BatchView& v, const BatchTuning& t, cudaStream_t st);
 cudaError_t launch_trace(const DScene& S, const double* rays, int64_t n, bool any, int* ids, double* t,
                          double* normals, cudaStream_t st);
 

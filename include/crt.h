@@ -297,12 +297,15 @@ crt_status crt_scene_check(crt_scene* scene, void* stream);
 
 /* ---- batched form: no counterpart in the reference, whose main loop
  * (src/main.cpp:300-330) builds and renders one mesh per process.  Many
- * meshes, each with its own camera, light and image size, are built by one
- * sequence of segmented kernels (the same Morton codes, sort, split search
- * and refit as crt_bvh_build, per mesh) and rendered by one persistent launch
- * whose warps claim (mesh, pixel tile) work items; crt_batch_run captures
- * that sequence once into a CUDA graph and replays it.  Every mesh's image
- * is what crt_render gives for that mesh alone. */
+ * meshes, each with its own camera, light and image size, are built and
+ * rendered by a persistent cooperative kernel: its phases (segmented
+ * bounds, Morton codes, sort, split search and refit -- the same as
+ * crt_bvh_build, per mesh -- then a render whose warps claim (mesh, pixel
+ * tile) work items) are separated by grid-wide barriers with bounded waits.
+ * The render runs in the same launch or in a persistent launch of its own
+ * (crt_batch_tuning.launches; the autotuner picks the faster).
+ * crt_batch_run captures the launches once into a CUDA graph and replays
+ * them.  Every mesh's image is what crt_render gives for that mesh alone. */
 typedef struct crt_batch crt_batch;
 
 typedef struct crt_batch_view {
@@ -311,14 +314,19 @@ typedef struct crt_batch_view {
   int32_t width, height, spp;
 } crt_batch_view;
 
-/* Launch shape of the batched pixel kernel: block_size in {64, 128, 256};
+/* Launch shape of the batch: block_size in {128, 256} threads (as many
+ * blocks as fit on the GPU at once);
  * lanes_per_pixel in {1, 2, 4, 8, 16, 32}: the most lanes (rays traced at
  * once) a pixel may take, capped by its samples per pixel, so a warp covers
  * 32 / lanes pixels; stack = traversal-stack entries kept in shared memory
- * per thread (0, 8, 16), the rest in local memory. */
+ * per thread (0, 8, 16), the rest in local memory; launches = 1: every
+ * build phase and the render in one persistent cooperative launch, 2: the
+ * build phases in one persistent cooperative launch and the render in a
+ * persistent launch of its own (both captured in the same graph). */
 typedef struct crt_batch_tuning {
   int32_t block_size, lanes_per_pixel, stack;
   float render_ms; /* written by crt_batch_autotune: the chosen shape's render time */
+  int32_t launches;
 } crt_batch_tuning;
 
 /* Host meshes and views (num_meshes <= 1024).  Copies everything to one
@@ -327,15 +335,15 @@ typedef struct crt_batch_tuning {
 crt_status crt_batch_create(const crt_mesh_desc* meshes, const crt_batch_view* views, int32_t num_meshes,
                             void* stream, crt_batch** out);
 crt_status crt_batch_destroy(crt_batch* batch);
-/* Build every mesh's BVH and render every view.  use_graph != 0 replays a
- * CUDA graph of the whole sequence (captured on the first such call after
- * create or a tuning change).  rgb8 (host or device, NULL to skip) receives
+/* Build every mesh's BVH and render every view (one or two launches).
+ * use_graph != 0 replays a CUDA graph of them (captured on the first such
+ * call after create or a tuning change).  rgb8 (host or device, NULL to skip) receives
  * the concatenated images; a host rgb8 synchronises `stream`. */
 crt_status crt_batch_run(crt_batch* batch, int32_t use_graph, uint8_t* rgb8, void* stream);
 crt_status crt_batch_set_tuning(crt_batch* batch, const crt_batch_tuning* tuning);
-/* Times the render under each supported tuning (one launch each after a
- * build and a warm-up render; lanes options that change no mesh's lanes per
- * pixel are skipped) and keeps the fastest. */
+/* Times the render phase under each supported tuning (one launch of that
+ * phase each, after a build and a warm-up render; lanes options that change
+ * no mesh's lanes per pixel are skipped) and keeps the fastest. */
 crt_status crt_batch_autotune(crt_batch* batch, crt_batch_tuning* chosen, void* stream);
 /* Mesh `mesh`'s build products in crt_bvh_export's layout (host or device
  * pointers; any may be NULL).  Synchronises `stream`. */

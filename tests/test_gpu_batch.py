@@ -1,6 +1,6 @@
 """Batched form: many meshes of uneven sizes, each with its own camera, light
-and image size, built by the segmented kernels and rendered by one persistent
-launch (replayed from a CUDA graph).  Every mesh's build products and image
+and image size, built and rendered by the persistent cooperative kernel (one
+launch, or the render in a second one; replayed from a CUDA graph).  Every mesh's build products and image
 must equal what the plain path gives for that mesh alone, bit for bit, for
 every supported launch shape; the plain path is itself pinned to the oracle
 (test_gpu_build, test_gpu_render), and a few meshes are checked against the
@@ -73,13 +73,14 @@ def test_batch_every_tuning_same_image(batch_case):
     ref = np.zeros((total, 3), np.uint8)
     b.set_tuning(128, 1, 0)
     b.run(ref, graph=False)
-    for bs in (64, 128, 256):
+    for bs in (128, 256):
         for lanes in (1, 2, 4, 8, 16, 32):
             for stack in (0, 8, 16):
-                b.set_tuning(bs, lanes, stack)
-                out = np.zeros_like(ref)
-                b.run(out, graph=bool(stack & 8))
-                assert_equal(out, ref, f"tuning {bs} lanes {lanes} stack {stack}")
+                for launches in (1, 2):
+                    b.set_tuning(bs, lanes, stack, launches)
+                    out = np.zeros_like(ref)
+                    b.run(out, graph=bool(stack & 8))
+                    assert_equal(out, ref, f"tuning {bs} lanes {lanes} stack {stack} launches {launches}")
     b.check()
 
 
@@ -90,8 +91,8 @@ def test_batch_graph_replay_and_autotune(batch_case):
     b.set_tuning(128, 4, 0)
     b.run(first, graph=False)
     t = b.autotune()
-    assert t["block_size"] in (64, 128, 256) and t["lanes_per_pixel"] in (1, 2, 4, 8, 16, 32)
-    assert t["stack"] in (0, 8, 16)
+    assert t["block_size"] in (128, 256) and t["lanes_per_pixel"] in (1, 2, 4, 8, 16, 32)
+    assert t["stack"] in (0, 8, 16) and t["launches"] in (1, 2)
     assert t["render_ms"] > 0
     for _ in range(3):  # replays of one captured graph
         again = np.zeros_like(first)
@@ -139,6 +140,12 @@ def test_batch_rejects_bad_input(cuda):
     bad.vidx[3, 1] = m.verts.shape[0]
     with pytest.raises(crt.CrtError, match="out of range"):
         crt.Batch([m, bad], [view, view])
+    b = crt.Batch([m, m], [view, view])
+    with pytest.raises(crt.CrtError, match="unsupported tuning"):
+        b.set_tuning(64, 4, 0)  # the persistent kernel runs 128- or 256-thread blocks
+    with pytest.raises(crt.CrtError, match="unsupported tuning"):
+        b.set_tuning(256, 4, 0, 3)
+    b.close()
     nan = data.Mesh(m.verts.copy(), m.vidx, m.normals, m.nidx, m.matid, m.materials)
     nan.verts[0, 0] = np.nan
     b = crt.Batch([m, nan], [view, view])
