@@ -77,54 +77,6 @@ struct BatchLaunch {
   int first, last;  // the phases to run
 };
 
-constexpr int kBarrierSpinLimit = 1 << 22;  // bounded barrier wait (x ~100 ns)
-
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ unsigned atom_add_acq_rel_u32(unsigned* p, unsigned v) {
-  unsigned old;
-  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
-  return old;
-}
-
-// Grid-wide barrier over all `nblocks` blocks: every write made before it by
-// any thread of the grid is visible to every thread after it.  Returns false
-// (and sets kErrTimeout) when the wait gave up; the caller then stops.
-__device__ __noinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* err) {
-  __shared__ int s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int ok = 1;
-    __threadfence();
-    const unsigned gen = ld_acquire_u32(bar + 1);
-    if (atom_add_acq_rel_u32(bar, 1u) == nblocks - 1) {
-      atomicExch(bar, 0u);
-      st_release_u32(bar + 1, gen + 1);
-    } else {
-      int spins = 0;
-      while (ld_acquire_u32(bar + 1) == gen) {
-        if (++spins > kBarrierSpinLimit ||
-            ((spins & 1023) == 0 && (ld_relaxed(reinterpret_cast<const uint32_t*>(err)) & kErrTimeout))) {
-          atomicOr(err, kErrTimeout);
-          ok = 0;
-          break;
-        }
-        __nanosleep(64);
-      }
-    }
-    __threadfence();
-    s_ok = ok;
-  }
-  __syncthreads();
-  return s_ok != 0;
-}
-
 __device__ __noinline__ void ph_init(const BatchBufs b) {
   const int M = b.M;
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {

@@ -175,6 +175,143 @@ __global__ void k_zero_u32(uint32_t* p, int n) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = 0;
 }
 
+// All passes of the build's stable LSD sort in one cooperative launch, one
+// 8192-key tile per block (so at most as many tiles as blocks that fit on the
+// GPU at once; launch_build falls back to k_onesweep passes beyond that).
+// Within a pass every block ranks its tile as k_onesweep does, publishes its
+// per-digit counts, and after a grid-wide barrier sums the counts of the
+// tiles before it (up to a few hundred independent loads per thread instead
+// of a chain of look-back round trips), then scatters; a second barrier ends
+// the pass.  Pass p reads keys_a (p even) or keys_b and writes the other
+// array (values likewise; pass 0 takes values 0..n-1).  Barrier words:
+// bar[0..1], zero at launch; a barrier that waits too long sets kErrTimeout
+// in *err and the kernel stops.
+template <int TH, int IT>
+__global__ void __launch_bounds__(TH, 1) k_sort_coop(uint32_t* keys_a, uint32_t* keys_b, uint32_t* vals_a,
+                                                     uint32_t* vals_b, int n, int passes,
+                                                     const uint32_t* __restrict__ hist, uint32_t* counts,
+                                                     unsigned* bar, int* err) {
+  constexpr int W = TH / 32;
+  constexpr int TILE = TH * IT;
+  constexpr int DPT = kRadix / TH;
+  static_assert(kRadix % TH == 0 && 32 * IT < 65536, "digits per thread, 16-bit warp counters");
+  __shared__ SortSmem<TH, IT> sm;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tile = blockIdx.x, ntiles = gridDim.x, base = tile * TILE;
+  const uint32_t mask = kRadix - 1;
+  unsigned short* wh = reinterpret_cast<unsigned short*>(sm.whist[warp]);
+  const uint32_t lt = lanemask_lt();
+  for (int p = 0; p < passes; p++) {
+    const uint32_t* kin = (p & 1) ? keys_b : keys_a;
+    const uint32_t* vin = p == 0 ? nullptr : ((p & 1) ? vals_b : vals_a);
+    uint32_t* kout = (p & 1) ? keys_a : keys_b;
+    uint32_t* vout = (p & 1) ? vals_a : vals_b;
+    const int shift = p * kRadixBits;
+    for (int i = tid; i < W * kRadix / 2; i += TH) (&sm.whist[0][0])[i] = 0;
+    uint32_t gh[DPT], gsum = 0;
+#pragma unroll
+    for (int j = 0; j < DPT; j++) gh[j] = __ldg(hist + p * kRadix + DPT * tid + j), gsum += gh[j];
+    uint32_t gtot;
+    const uint32_t gpre = block_excl_scan<TH>(gsum, sm.warp, gtot);
+    // rank the tile's keys in input order (stable), warp by warp
+    uint32_t key[IT], val[IT], rank[IT];
+#pragma unroll
+    for (int r = 0; r < IT; r++) {  // every load issued before the ranking's warp syncs
+      const int idx = base + warp * (32 * IT) + r * 32 + lane;
+      const bool valid = idx < n;
+      key[r] = valid ? ld_in<false>(kin + idx) : 0u;
+      val[r] = valid ? (vin ? ld_in<false>(vin + idx) : (uint32_t)idx) : 0u;
+    }
+#pragma unroll
+    for (int r = 0; r < IT; r++) {
+      const int idx = base + warp * (32 * IT) + r * 32 + lane;
+      const bool valid = idx < n;
+      const uint32_t d = valid ? ((key[r] >> shift) & mask) : (uint32_t)kRadix;
+      const uint32_t peers = digit_peers(d, valid);
+      const int leader = __ffs(peers) - 1;
+      uint32_t b = 0;
+      if (lane == leader && valid) {
+        b = wh[d];
+        wh[d] = (unsigned short)(b + __popc(peers));
+      }
+      b = __shfl_sync(0xffffffffu, b, leader);
+      rank[r] = b + __popc(peers & lt);
+      __syncwarp();
+    }
+    __syncthreads();
+    // per digit: warp offsets (exclusive, in place) and the tile's count
+    uint32_t cnt[DPT], csum = 0;
+#pragma unroll
+    for (int j = 0; j < DPT; j++) {
+      const int d = DPT * tid + j;
+      uint32_t c = 0;
+#pragma unroll
+      for (int w = 0; w < W; w++) {
+        unsigned short* h = reinterpret_cast<unsigned short*>(sm.whist[w]) + d;
+        const uint32_t x = *h;
+        *h = (unsigned short)c;
+        c += x;
+      }
+      cnt[j] = c;
+      csum += c;
+    }
+    uint32_t* mine = counts + ((size_t)p * ntiles + tile) * kRadix;
+#pragma unroll
+    for (int j = 0; j < DPT; j++) mine[DPT * tid + j] = cnt[j];
+    if (!grid_barrier(bar, ntiles, err)) return;
+    // each digit's count over the tiles before this one
+    uint32_t pre[DPT];
+#pragma unroll
+    for (int j = 0; j < DPT; j++) {
+      const uint32_t* col = counts + (size_t)p * ntiles * kRadix + DPT * tid + j;
+      // 32 loads in flight per round (each round waits one L2 round trip)
+      constexpr int U = 32;
+      uint32_t acc = 0u;
+      for (int t0 = 0; t0 < tile; t0 += U) {
+        uint32_t x[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) x[u] = t0 + u < tile ? __ldcg(col + (size_t)(t0 + u) * kRadix) : 0u;
+#pragma unroll
+        for (int u = 0; u < U; u++) acc += x[u];
+      }
+      pre[j] = acc;
+    }
+    uint32_t ctot;
+    const uint32_t cpre = block_excl_scan<TH>(csum, sm.warp, ctot);
+    {
+      uint32_t c = cpre, g = gpre;
+#pragma unroll
+      for (int j = 0; j < DPT; j++) {
+        const int d = DPT * tid + j;
+        sm.tstart[d] = c;
+        sm.gbase[d] = g + pre[j] - c;
+        c += cnt[j];
+        g += gh[j];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < IT; r++) {
+      const int idx = base + warp * (32 * IT) + r * 32 + lane;
+      if (idx < n) {
+        const uint32_t d = (key[r] >> shift) & mask;
+        const uint32_t pos = sm.tstart[d] + wh[d] + rank[r];
+        sm.keys[pos] = key[r];
+        sm.vals[pos] = val[r];
+      }
+    }
+    __syncthreads();
+    const int tile_n = min(TILE, n - base);
+    for (int i = tid; i < tile_n; i += TH) {
+      const uint32_t k = sm.keys[i];
+      const uint32_t pos = sm.gbase[(k >> shift) & mask] + (uint32_t)i;
+      kout[pos] = k;
+      vout[pos] = sm.vals[i];
+    }
+    if (p + 1 < passes && !grid_barrier(bar, ntiles, err)) return;
+  }
+}
+
 // BuildHierarchy (kernels/bvh.cu:164-207) with FindSpan (bvh.cu:100-133) and
 // FindSplit (bvh.cu:134-162): one thread per internal node writes its
 // children's parent words and clears the node's refit flag (the child codes
@@ -492,28 +629,61 @@ static void refit(const MeshBufs& m, const BuildBufs& b, cudaStream_t st) {
              (const uint32_t*)b.arrivals, n, b.flags, b.g);
 }
 
+// Whether the build's sort runs as one cooperative launch (k_sort_coop): its
+// 8192-key tiles must all be resident at once.
+static bool coop_sort_fits(int n) {
+  static int capacity = -1;
+  if (capacity < 0) {
+    int bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_sort_coop<kSortThreadsL, kSortItems>, kSortThreadsL, 0) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      bps = 0;
+    }
+    capacity = bps * num_sms();
+  }
+  return n >= 2 * kSortTileL && (n + kSortTileL - 1) / kSortTileL <= capacity;
+}
+
 cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st) {
   const int n = m.ntri;
   if (n <= 0) return cudaSuccess;
   const int passes = 3;
   const int tiles = sort_tiles(n);
+  const bool coop = coop_sort_fits(n);
   k_build_init<<<1, 1024, 0, st>>>(b.g, b.hist, passes * kRadix);
   const int sms = num_sms();
   const int gb = min((n + 255) / 256, sms * 8);
   launch_k(true, k_bounds, gb, 256, st, (const float*)m.verts, (const int*)m.vidx, n, b.g);
   const int gm = min((n + 511) / 512, sms * 2);
+  // (the look-back status is cleared only for the passes that use it)
   launch_k(true, k_morton, gm, 512, st, (const float*)m.verts, (const int*)m.vidx, n, (const SceneGlobals*)b.g,
-           b.keys_a, b.hist, passes, b.status, passes * tiles * kRadix);
+           b.keys_a, b.hist, passes, b.status, coop ? 0 : passes * tiles * kRadix);
   // pass 0: keys_a -> keys_b (values 0..n-1), pass 1: b -> a, pass 2: a -> b
-  const uint32_t* kin = b.keys_a;
-  const uint32_t* vin = nullptr;
-  for (int p = 0; p < passes; p++) {
-    uint32_t* ko = (p & 1) ? b.keys_a : b.keys_b;
-    uint32_t* vo = (p & 1) ? b.vals_a : b.vals_b;
-    onesweep_pass(kin, vin, ko, vo, n, p * kRadixBits, b.hist + p * kRadix, b.status + (size_t)p * tiles * kRadix,
-                  &b.g->tile_counter[p], &b.g->err, st, true);
-    kin = ko;
-    vin = vo;
+  if (coop) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)((n + kSortTileL - 1) / kSortTileL));
+    cfg.blockDim = dim3(kSortThreadsL);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    // barrier words: tile_counter[0..1], zeroed by k_build_init
+    cudaLaunchKernelEx(&cfg, k_sort_coop<kSortThreadsL, kSortItems>, b.keys_a, b.keys_b, b.vals_a, b.vals_b, n,
+                       passes, (const uint32_t*)b.hist, b.status, &b.g->tile_counter[0], &b.g->err);
+  } else {
+    const uint32_t* kin = b.keys_a;
+    const uint32_t* vin = nullptr;
+    for (int p = 0; p < passes; p++) {
+      uint32_t* ko = (p & 1) ? b.keys_a : b.keys_b;
+      uint32_t* vo = (p & 1) ? b.vals_a : b.vals_b;
+      onesweep_pass(kin, vin, ko, vo, n, p * kRadixBits, b.hist + p * kRadix, b.status + (size_t)p * tiles * kRadix,
+                    &b.g->tile_counter[p], &b.g->err, st, true);
+      kin = ko;
+      vin = vo;
+    }
   }
   if (n >= 2)
     launch_k(true, k_hierarchy, (n - 1 + kHierThreads - 1) / kHierThreads, kHierThreads, st,

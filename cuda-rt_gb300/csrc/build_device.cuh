@@ -189,10 +189,73 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_warp
 
 constexpr uint32_t kFlagAgg = 1u << 30, kFlagInc = 2u << 30, kValMask = (1u << 30) - 1;
 
+constexpr int kBarrierSpinLimit = 1 << 22;  // bounded barrier wait (x ~100 ns)
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned atom_add_acq_rel_u32(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
+
+// Grid-wide barrier over all `nblocks` blocks: every write made before it by
+// any thread of the grid is visible to every thread after it.  Returns false
+// (and sets kErrTimeout) when the wait gave up; the caller then stops.
+__device__ __noinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* err) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    __threadfence();
+    const unsigned gen = ld_acquire_u32(bar + 1);
+    if (atom_add_acq_rel_u32(bar, 1u) == nblocks - 1) {
+      atomicExch(bar, 0u);
+      st_release_u32(bar + 1, gen + 1);
+    } else {
+      int spins = 0;
+      while (ld_acquire_u32(bar + 1) == gen) {
+        if (++spins > kBarrierSpinLimit ||
+            ((spins & 1023) == 0 && (ld_relaxed(reinterpret_cast<const uint32_t*>(err)) & kErrTimeout))) {
+          atomicOr(err, kErrTimeout);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// The lanes of the warp whose key has digit d (a 10-bit digit; lanes with
+// valid false take part in the votes and match no one): one ballot per digit
+// bit, each lane keeping the lanes that agree with it on every bit.  (This
+// replaces __match_any_sync, whose issue cost made it the sort's bottleneck.)
+__device__ __forceinline__ uint32_t digit_peers(uint32_t d, bool valid) {
+  uint32_t peers = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+  for (int b = 0; b < kRadixBits; b++) {
+    const bool bit = (d >> b) & 1u;
+    const uint32_t vote = __ballot_sync(0xffffffffu, bit);
+    peers &= bit ? vote : ~vote;
+  }
+  return peers;
+}
+
 // One stable LSD pass over the digit at `shift` (thrust::sort_by_key's
 // role, kernels/bvh.cu:267-273).  Tiles of TH * IT keys are claimed in order
 // from an atomic counter; within a tile, warps rank their 32 * IT keys in
-// input order with __match_any_sync, and the tile's digit offsets come from a
+// input order (digit_peers), and the tile's digit offsets come from a
 // decoupled look-back over the tiles before it.  Two shapes (sort_large):
 // 2048-key tiles of 256 threads for small inputs, 8192-key tiles of 1024
 // threads from 2^19 keys on (a quarter of the tiles, so a quarter of the
@@ -245,13 +308,18 @@ __device__ __forceinline__ void onesweep_tile(SortSmem<TH, IT, STAGE>& sm, int t
   unsigned short* wh = reinterpret_cast<unsigned short*>(s_whist[warp]);
   const uint32_t lt = lanemask_lt();
 #pragma unroll
-  for (int r = 0; r < IT; r++) {
+  for (int r = 0; r < IT; r++) {  // every load issued before the ranking's warp syncs
     const int idx = base + warp * (32 * IT) + r * 32 + lane;
     const bool valid = idx < n;
     key[r] = valid ? ld_in<NC>(kin + idx) : 0u;
     val[r] = valid ? (vin ? ld_in<NC>(vin + idx) : (uint32_t)idx) : 0u;
+  }
+#pragma unroll
+  for (int r = 0; r < IT; r++) {
+    const int idx = base + warp * (32 * IT) + r * 32 + lane;
+    const bool valid = idx < n;
     const uint32_t d = valid ? ((key[r] >> shift) & mask) : (uint32_t)kRadix;
-    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t peers = digit_peers(d, valid);
     const int leader = __ffs(peers) - 1;
     uint32_t b = 0;
     if (lane == leader && valid) {
