@@ -41,14 +41,30 @@ sys.path.insert(0, ROOT)
 
 METRIC = "LBVH build Mtris/s; closest-hit Mrays/s; batched+adjoint vs plain, 1 GB300"
 W, H, SPP = 1920, 1080, 16
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one k_pixels
-# launch of this frame, from an ncu --set full capture of this command (of the
-# instrumented launch, the same kernel with traversal counters); the
-# fetched bytes (the `achieved` numerator) are mostly served by L1 and L2.
-# Most of these bytes are the lens-table lookups (two random loads per
-# sample, each filling whole L2 lines) and the threads' local memory
-# (traversal stacks and register spills of 175,104 resident threads).
-RENDER_DRAM_BYTES = 12_587_523_328
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one timed
+# k_pixels launch of this frame (9,606,780,416 read + 2,594,846,720 written),
+# and the build's DRAM and L2 (lts__t_bytes.sum) bytes summed over its seven
+# kernels, from single-pass ncu captures (profiles/large_frame_step_kernels.md
+# gives the commands); the render's fetched bytes (the `achieved` numerator)
+# are mostly served by L1 and L2.  Most of the render's DRAM bytes are the
+# lens-table lookups (two random loads per sample, each filling whole L2
+# lines) and the threads' local memory (traversal stacks and register spills
+# of 175,104 resident threads).  Re-captured whenever those kernels change.
+RENDER_DRAM_BYTES = 12_201_627_136
+BUILD_DRAM_BYTES = 225_798_912
+BUILD_L2_BYTES = 879_124_640
+TRAFFIC_SOURCE = "ncu 2025.3 single-pass captures, GB300, 2026-12-04"
+
+
+def build_launches(n):
+    """Kernel launches of one crt_bvh_build of n triangles (build.cu): init,
+    bounds, Morton, the sort (one cooperative launch from 16,384 triangles
+    up to 152 tiles of 8192, else three passes), split search, refit and,
+    above one 512-leaf refit block, the spanning-node refit."""
+    if n <= 0:
+        return 0
+    sort = 1 if 2 * 8192 <= n <= 152 * 8192 else 3
+    return 3 + sort + (1 if n >= 2 else 0) + 1 + (1 if n > 512 else 0)
 
 
 def peaks():
@@ -245,14 +261,16 @@ def run_crt(args, dist, rank, ws):
         "render_ms": round(render_s * 1e3, 3), "render_mrays_s": round(rays / render_s / 1e6, 2),
         "build_roofline": {"bound": "hbm", "achieved": round(build_bytes / build_s / 1e9, 1), "peak": hbm,
                            "unit": "GB/s", "frac": round(build_bytes / build_s / 1e9 / hbm, 4),
-                           "bytes_per_tri": round(s_in + 220, 1), "peak_kind": peak_kind},
+                           "bytes_per_tri": round(s_in + 220, 1), "peak_kind": peak_kind,
+                           "traffic": BUILD_DRAM_BYTES, "l2_bytes": BUILD_L2_BYTES,
+                           "l2_gbs": round(BUILD_L2_BYTES / build_s / 1e9, 1), "traffic_source": TRAFFIC_SOURCE},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "traffic": RENDER_DRAM_BYTES, "kernel": "k_pixels",
                      "alg_bytes_per_launch": alg_bytes, "nodes_visited": nodes_visited,
-                     "tris_tested": tris_tested, "peak_kind": peak_kind},
+                     "tris_tested": tris_tested, "peak_kind": peak_kind, "traffic_source": TRAFFIC_SOURCE},
         "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": int(mesh.verts.nbytes),
                 "d2h_bytes_per_step": W * H * 3, "image_matches_device_run": ok_img},
-        "gpu_launches": 9 * args.steps,
+        "gpu_launches": (build_launches(n) + 1) * args.steps,
         "clocks": clk.summary(),
     }
     if refit is not None:
@@ -266,6 +284,60 @@ def run_crt(args, dist, rank, ws):
     if cpu is not None:
         line["cpu_baseline"] = cpu
     return line
+
+
+def run_build_only(args):
+    """crt_bvh_build of the large mesh, W untimed then K timed back to back
+    (CUDA events on the library's stream); the device holds the scene only
+    (about 300 MB), which keeps ncu captures of the build kernels small."""
+    import torch
+
+    import crt
+    from crt import data
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    sc = data.config1()
+    scene = crt.Scene(sc.mesh)
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        scene.build(stream=stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        scene.build(stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    scene.check()
+    ms = e0.elapsed_time(e1) / max(args.steps, 1)
+    n = sc.mesh.ntri
+    return {"metric": "LBVH build ms (large mesh, back to back)", "value": round(ms, 4), "unit": "ms",
+            "higher_is_better": False, "steps": args.steps, "warmup": args.warmup, "triangles": n,
+            "build_mtris_s": round(n / ms / 1e3, 1), "gpu_launches": build_launches(n) * args.steps}
+
+
+def run_batched_only(count):
+    """The first `count` meshes of the batched workload, built and rendered
+    twice in the two-launch form with a fixed shape; the second run timed."""
+    import torch
+
+    import crt
+    from crt import data
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    scs = data.config3(count=count)
+    b = crt.Batch([s.mesh for s in scs], [(s.camera, s.light, s.width, s.height, s.spp) for s in scs])
+    img = torch.empty((int(b.offsets[-1]), 3), dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    b.set_tuning(256, 1, 16, 2)
+    b.run(img, graph=False, stream=stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.run(img, graph=False, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    b.check()
+    ms = e0.elapsed_time(e1)
+    return {"metric": "batched build + render ms", "value": round(ms, 3), "unit": "ms", "higher_is_better": False,
+            "meshes": count, "triangles": sum(b.ntri), "rays": b.rays, "mrays_s": round(b.rays / ms / 1e3, 1)}
 
 
 def run_refit_vs_rebuild(frames=60, W2=1280, H2=720, spp=4):
@@ -373,6 +445,16 @@ def run_batched(count=256, reps=3):
     torch.cuda.synchronize()
     t_plain = timed(plain)
     same = bool(torch.equal(img_b, img_p))
+    # traversal work per primary ray of this workload (the same walks as the
+    # batched render's), from instrumented plain renders, untimed
+    stats = torch.zeros(2, dtype=torch.int64, device="cuda")
+    total = torch.zeros(2, dtype=torch.int64, device="cuda")
+    for m, s in enumerate(scs):  # (each render clears the counters it is given)
+        scenes[m].render(s.camera, s.light, s.width, s.height, s.spp, out={"rgb8": img_p[b.offsets[m]:b.offsets[m + 1]],
+                                                                           "traversal_stats": stats}, stream=stream)
+        total += stats
+    torch.cuda.synchronize()
+    nodes, tested = (int(x) for x in total.cpu())
     for s in scenes:
         s.check()
         s.close()
@@ -381,7 +463,8 @@ def run_batched(count=256, reps=3):
             "batched_ms": round(t_batch, 3), "plain_ms": round(t_plain, 3),
             "batched_mrays_s": round(rays / t_batch / 1e3, 1), "plain_mrays_s": round(rays / t_plain / 1e3, 1),
             "speedup": round(t_plain / t_batch, 3), "tuning": tune, "images_identical": same and same_forms,
-            "plain_launches": 9 * count, "batched_launches": tune["launches"],
+            "plain_launches": sum(build_launches(t) + 1 for t in b.ntri), "batched_launches": tune["launches"],
+            "nodes_per_ray": round(nodes / rays, 2), "tris_per_ray": round(tested / rays, 2),
             f"{other}_launch_form_ms": round(t_other, 3)}
 
 
@@ -631,6 +714,11 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the refit-vs-rebuild, batched-vs-plain, adjoint and next-row figures")
+    ap.add_argument("--batched-only", type=int, default=0, metavar="MESHES",
+                    help="build and render the first MESHES meshes of the batched workload twice, two launches "
+                         "each (block 256, 1 lane per pixel, stack 16), and time the second run: for profiling")
+    ap.add_argument("--build-only", action="store_true",
+                    help="time the LBVH build of the large mesh alone (no render, no lens tables): for profiling it")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "crt" else args.warmup
     dist, rank, ws = dist_setup()
@@ -641,7 +729,12 @@ def main():
         if rank == 0:
             __graft_entry__.build()
         barrier(dist)
-        line = run_crt(args, dist, rank, ws)
+        if args.build_only:
+            line = run_build_only(args)
+        elif args.batched_only:
+            line = run_batched_only(args.batched_only)
+        else:
+            line = run_crt(args, dist, rank, ws)
     if rank == 0 and line is not None:
         print(json.dumps(line), flush=True)
     if dist is not None:
