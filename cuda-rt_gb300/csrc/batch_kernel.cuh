@@ -150,10 +150,11 @@ __device__ __noinline__ void ph_morton(const BatchBufs b, int sort_tiles, uint32
   __syncthreads();
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x) {
     float3 a, bb, c;
-    float lo[3], hi[3], mn[3], mx[3];
+    float lo[3], hi[3];
+    MortonAxis ax[3];
     tri_box(b.verts, b.vidx, t, a, bb, c, lo, hi);
-    load_scene_box(b.g + __ldg(b.mesh_of + t), mn, mx);
-    const uint32_t code = morton_code(lo, hi, mn, mx);
+    load_scene_box(b.g + __ldg(b.mesh_of + t), ax);
+    const uint32_t code = morton_code(lo, hi, ax);
     b.keys_a[t] = code;
     b.codes0[t] = code;
     for (int p = 0; p < 3; p++) atomicAdd(&sh[p * kRadix + ((code >> (p * kRadixBits)) & (kRadix - 1))], 1u);

@@ -4,8 +4,11 @@
 // src/bvh.cpp:3-32):
 //   k_build_init   reset the per-scene globals and sort histograms
 //   k_bounds       triangle AABBs reduced to the scene box (findMinMax)
-//   k_morton       30-bit Morton codes + the digit histograms of all sort passes
-//   k_onesweep x3  stable LSD radix sort, 10-bit digits, decoupled look-back
+//   k_morton       30-bit Morton codes (+ the digit histograms of the sort
+//                  passes when they run as look-back passes)
+//   k_sort_coop    stable LSD radix sort, 10-bit digits, all three passes in
+//                  one cooperative launch (or k_onesweep x3, decoupled
+//                  look-back, when the tiles do not all fit at once)
 //   k_hierarchy    Karras split search, one thread per internal node
 //   k_refit        atomic bottom-up refit, one climber per leaf; it also
 //                  writes the leaf triangles in sorted order for traversal
@@ -19,10 +22,16 @@ namespace crt {
 
 namespace {
 
-__global__ void k_build_init(SceneGlobals* g, uint32_t* hist, int nhist) {
+// Empty group boxes for k_refit's atomic min/max (order-preserving ints).
+__device__ __forceinline__ void clear_group_boxes(int* gbox, int groups) {
+  for (int i = threadIdx.x; i < 6 * groups; i += blockDim.x) gbox[i] = f2ord(i % 6 < 3 ? INFINITY : -INFINITY);
+}
+
+__global__ void k_build_init(SceneGlobals* g, uint32_t* hist, int nhist, int* gbox, int groups) {
   pdl_wait();
   pdl_launch_dependents();
   const int t = threadIdx.x;
+  clear_group_boxes(gbox, groups);
   if (t < 3) {
     g->bmin[t] = f2ord(1e9f);  // findMinMax's initial values (kernels/scene.cu:75,80)
     g->bmax[t] = f2ord(-1e9f);
@@ -30,7 +39,7 @@ __global__ void k_build_init(SceneGlobals* g, uint32_t* hist, int nhist) {
   if (t == 0) {
     g->emax = f2ord(0.f);
     g->err = 0;
-    g->narr = 0u;
+    g->nspan = 0u;
   }
   if (t < 4) g->tile_counter[t] = 0;
   for (int i = t; i < nhist; i += blockDim.x) hist[i] = 0;
@@ -91,22 +100,26 @@ __global__ void __launch_bounds__(256) k_bounds(const float* __restrict__ V, con
   if (threadIdx.x == 0 && s_bad) atomicOr(&g->err, kErrNonFinite);
 }
 
-// Morton codes + per-pass digit histograms; also clears the look-back status.
-// (Counting each digit once per group of lanes that share it, with
-// __match_any_sync, measured 31 us against 25 us for per-lane shared atomics
-// on the 1M-triangle build.)
+// Morton codes; with HIST also the digit histograms of the sort passes (the
+// look-back passes need them; the cooperative sort counts its digits itself)
+// and the look-back status cleared.  (Counting each digit once per group of
+// lanes that share it, with __match_any_sync, measured 31 us against 25 us
+// for per-lane shared atomics on the 1M-triangle build.)
+template <bool HIST>
 __global__ void __launch_bounds__(512, 2) k_morton(const float* __restrict__ V, const int* __restrict__ vidx, int n,
-                                                const SceneGlobals* g, uint32_t* __restrict__ keys,
-                                                uint32_t* __restrict__ hist, int passes,
-                                                uint32_t* __restrict__ status, int status_words) {
-  __shared__ uint32_t sh[3 * kRadix];
-  for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) sh[i] = 0;
+                                                   const SceneGlobals* g, uint32_t* __restrict__ keys,
+                                                   uint32_t* __restrict__ hist, int passes,
+                                                   uint32_t* __restrict__ status, int status_words) {
+  __shared__ uint32_t sh[HIST ? 3 * kRadix : 1];
+  if (HIST)
+    for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) sh[i] = 0;
   pdl_wait();
   pdl_launch_dependents();
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < status_words; i += gridDim.x * blockDim.x) status[i] = 0;
-  float mn[3], mx[3];
-  load_scene_box(g, mn, mx);
-  __syncthreads();
+  if (HIST)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < status_words; i += gridDim.x * blockDim.x) status[i] = 0;
+  MortonAxis ax[3];
+  load_scene_box(g, ax);
+  if (HIST) __syncthreads();
   // four triangles per thread per round: their loads overlap
   const int stride = gridDim.x * blockDim.x;
   for (int t0 = blockIdx.x * blockDim.x + threadIdx.x; t0 < n; t0 += 4 * stride) {
@@ -121,16 +134,19 @@ __global__ void __launch_bounds__(512, 2) k_morton(const float* __restrict__ V, 
     for (int u = 0; u < 4; u++) {
       const int t = t0 + u * stride;
       if (t < n) {
-        const uint32_t code = morton_code(lo[u], hi[u], mn, mx);
+        const uint32_t code = morton_code(lo[u], hi[u], ax);
         keys[t] = code;
-        for (int p = 0; p < passes; p++)
-          atomicAdd(&sh[p * kRadix + ((code >> (p * kRadixBits)) & (kRadix - 1))], 1u);
+        if (HIST)
+          for (int p = 0; p < passes; p++)
+            atomicAdd(&sh[p * kRadix + ((code >> (p * kRadixBits)) & (kRadix - 1))], 1u);
       }
     }
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x)
-    if (sh[i]) atomicAdd(&hist[i], sh[i]);
+  if (HIST) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x)
+      if (sh[i]) atomicAdd(&hist[i], sh[i]);
+  }
 }
 
 // Standalone Morton codes against a given scene box (crt_morton).  A
@@ -138,9 +154,9 @@ __global__ void __launch_bounds__(512, 2) k_morton(const float* __restrict__ V, 
 // vertices are not read.
 __global__ void k_morton_only(const float* __restrict__ V, int nv, const int* __restrict__ vidx, int n,
                               const float* __restrict__ box6, uint32_t* __restrict__ keys, int* err) {
-  float mn[3], mx[3];
+  MortonAxis ax[3];
 #pragma unroll
-  for (int k = 0; k < 3; k++) mn[k] = box6[k], mx[k] = box6[3 + k];
+  for (int k = 0; k < 3; k++) ax[k] = morton_axis_setup(box6[k], box6[3 + k]);
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     if ((unsigned)__ldg(vidx + 3 * t) >= (unsigned)nv || (unsigned)__ldg(vidx + 3 * t + 1) >= (unsigned)nv ||
         (unsigned)__ldg(vidx + 3 * t + 2) >= (unsigned)nv) {
@@ -151,7 +167,7 @@ __global__ void k_morton_only(const float* __restrict__ V, int nv, const int* __
     float3 a, b, c;
     float lo[3], hi[3];
     tri_box(V, vidx, t, a, b, c, lo, hi);
-    keys[t] = morton_code(lo, hi, mn, mx);
+    keys[t] = morton_code(lo, hi, ax);
   }
 }
 
@@ -179,17 +195,17 @@ __global__ void k_zero_u32(uint32_t* p, int n) {
 // 8192-key tile per block (so at most as many tiles as blocks that fit on the
 // GPU at once; launch_build falls back to k_onesweep passes beyond that).
 // Within a pass every block ranks its tile as k_onesweep does, publishes its
-// per-digit counts, and after a grid-wide barrier sums the counts of the
-// tiles before it (up to a few hundred independent loads per thread instead
-// of a chain of look-back round trips), then scatters; a second barrier ends
-// the pass.  Pass p reads keys_a (p even) or keys_b and writes the other
+// per-digit counts, and after a grid-wide barrier sums the counts of all
+// tiles, keeping apart those of the tiles before it (up to a few hundred
+// independent loads per thread instead of a chain of look-back round trips):
+// the digit totals give each digit's start, so no histogram pass precedes the
+// sort.  Then it scatters; a second barrier ends the pass.  Pass p reads keys_a (p even) or keys_b and writes the other
 // array (values likewise; pass 0 takes values 0..n-1).  Barrier words:
 // bar[0..1], zero at launch; a barrier that waits too long sets kErrTimeout
 // in *err and the kernel stops.
 template <int TH, int IT>
 __global__ void __launch_bounds__(TH, 1) k_sort_coop(uint32_t* keys_a, uint32_t* keys_b, uint32_t* vals_a,
-                                                     uint32_t* vals_b, int n, int passes,
-                                                     const uint32_t* __restrict__ hist, uint32_t* counts,
+                                                     uint32_t* vals_b, int n, int passes, uint32_t* counts,
                                                      unsigned* bar, int* err) {
   constexpr int W = TH / 32;
   constexpr int TILE = TH * IT;
@@ -207,12 +223,10 @@ __global__ void __launch_bounds__(TH, 1) k_sort_coop(uint32_t* keys_a, uint32_t*
     uint32_t* kout = (p & 1) ? keys_a : keys_b;
     uint32_t* vout = (p & 1) ? vals_a : vals_b;
     const int shift = p * kRadixBits;
-    for (int i = tid; i < W * kRadix / 2; i += TH) (&sm.whist[0][0])[i] = 0;
-    uint32_t gh[DPT], gsum = 0;
-#pragma unroll
-    for (int j = 0; j < DPT; j++) gh[j] = __ldg(hist + p * kRadix + DPT * tid + j), gsum += gh[j];
-    uint32_t gtot;
-    const uint32_t gpre = block_excl_scan<TH>(gsum, sm.warp, gtot);
+    // each warp clears its own counters (no other warp reads them before the
+    // block's next __syncthreads)
+    for (int i = lane; i < kRadix / 2; i += 32) sm.whist[warp][i] = 0;
+    __syncwarp();
     // rank the tile's keys in input order (stable), warp by warp
     uint32_t key[IT], val[IT], rank[IT];
 #pragma unroll
@@ -259,25 +273,33 @@ __global__ void __launch_bounds__(TH, 1) k_sort_coop(uint32_t* keys_a, uint32_t*
 #pragma unroll
     for (int j = 0; j < DPT; j++) mine[DPT * tid + j] = cnt[j];
     if (!grid_barrier(bar, ntiles, err)) return;
-    // each digit's count over the tiles before this one
-    uint32_t pre[DPT];
+    // each digit's count over the tiles before this one, and over all tiles
+    // (every block reads every tile's counts: no longer than the last
+    // block's prefix alone, which the pass waits for anyway)
+    uint32_t pre[DPT], tot[DPT], gsum = 0;
 #pragma unroll
     for (int j = 0; j < DPT; j++) {
       const uint32_t* col = counts + (size_t)p * ntiles * kRadix + DPT * tid + j;
       // 32 loads in flight per round (each round waits one L2 round trip)
       constexpr int U = 32;
-      uint32_t acc = 0u;
-      for (int t0 = 0; t0 < tile; t0 += U) {
+      uint32_t acc = 0u, all = 0u;
+      for (int t0 = 0; t0 < ntiles; t0 += U) {
         uint32_t x[U];
 #pragma unroll
-        for (int u = 0; u < U; u++) x[u] = t0 + u < tile ? __ldcg(col + (size_t)(t0 + u) * kRadix) : 0u;
+        for (int u = 0; u < U; u++) x[u] = t0 + u < ntiles ? __ldcg(col + (size_t)(t0 + u) * kRadix) : 0u;
 #pragma unroll
-        for (int u = 0; u < U; u++) acc += x[u];
+        for (int u = 0; u < U; u++) {
+          all += x[u];
+          acc += t0 + u < tile ? x[u] : 0u;
+        }
       }
       pre[j] = acc;
+      tot[j] = all;
+      gsum += all;
     }
-    uint32_t ctot;
-    const uint32_t cpre = block_excl_scan<TH>(csum, sm.warp, ctot);
+    // digit starts (over all keys) and tile-local digit starts, in one scan
+    uint32_t gpre, cpre;
+    block_excl_scan2<TH>(gsum, csum, sm.warp2, gpre, cpre);
     {
       uint32_t c = cpre, g = gpre;
 #pragma unroll
@@ -286,7 +308,7 @@ __global__ void __launch_bounds__(TH, 1) k_sort_coop(uint32_t* keys_a, uint32_t*
         sm.tstart[d] = c;
         sm.gbase[d] = g + pre[j] - c;
         c += cnt[j];
-        g += gh[j];
+        g += tot[j];
       }
     }
     __syncthreads();
@@ -314,9 +336,10 @@ __global__ void __launch_bounds__(TH, 1) k_sort_coop(uint32_t* keys_a, uint32_t*
 
 // BuildHierarchy (kernels/bvh.cu:164-207) with FindSpan (bvh.cu:100-133) and
 // FindSplit (bvh.cu:134-162): one thread per internal node writes its
-// children's parent words and clears the node's refit flag (the child codes
-// and boxes reach the wide nodes through the refit, which relies on the
-// empty odd slot marked here beside a leaf child).  Every probe of a node
+// children's parent words and lists its spanning children for
+// k_refit_spans (the child codes and boxes reach the wide nodes through the
+// refit, which relies on the empty odd slot marked here beside a leaf
+// child).  Every probe of a node
 // whose span is at most kShortSpan leaves lies within kShortSpan of the node,
 // so a block first stages the codes of its nodes +- kShortSpan in shared
 // memory (one coalesced load) and searches there.  A node whose span turns
@@ -338,8 +361,8 @@ __device__ __forceinline__ int kdelta_s(const uint32_t* s_c, int w0, int n, uint
 }
 
 __global__ void __launch_bounds__(kHierThreads) k_hierarchy(const uint32_t* __restrict__ codes, int n,
-                                                            uint32_t* __restrict__ parent, int* __restrict__ flags,
-                                                            WNode* __restrict__ wnodes) {
+                                                            uint32_t* __restrict__ parent, WNode* __restrict__ wnodes,
+                                                            uint4* __restrict__ spans, unsigned* nspan) {
   __shared__ uint32_t s_c[kHierWindow];
   pdl_wait();
   pdl_launch_dependents();
@@ -398,93 +421,156 @@ __global__ void __launch_bounds__(kHierThreads) k_hierarchy(const uint32_t* __re
     const int o = warp_prefix_end(hiL - loL - 1, [&](int m) { return kdelta(codes, n, klo, loL + m) > same; });
     if (lane == L) lo = loL, hi = hiL, split = loL + o;
   }
-  if (!act) return;
   const int c1 = (split == lo) ? ~split : split;
   const int c2 = (split + 1 == hi) ? ~(split + 1) : split + 1;
-  const uint32_t spans = (lo / kRefitBlock != hi / kRefitBlock) ? kParentSpans : 0u;
-  parent[c1 < 0 ? (n - 1) + split : split] = (uint32_t)i | kParentLeft | spans;
-  parent[c2 < 0 ? (n - 1) + split + 1 : split + 1] = (uint32_t)i | spans;
-  flags[i] = 0;
+  if (spans) {
+    // the spanning children (internal nodes whose leaf range crosses a
+    // kRefitBlock boundary) join the list k_refit_spans works through:
+    // (node, first leaf, last leaf, parent word)
+    const bool s1 = act && c1 >= 0 && lo / kRefitBlock != split / kRefitBlock;
+    const bool s2 = act && c2 >= 0 && (split + 1) / kRefitBlock != hi / kRefitBlock;
+    const uint32_t m1 = __ballot_sync(0xffffffffu, s1), m2 = __ballot_sync(0xffffffffu, s2);
+    if (m1 | m2) {
+      unsigned base = 0;
+      if (lane == 0) base = atomicAdd(nspan, (unsigned)(__popc(m1) + __popc(m2)));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      const uint32_t lt = lanemask_lt();
+      const uint32_t pw = (uint32_t)i | ((lo / kRefitBlock != hi / kRefitBlock) ? kParentSpans : 0u);
+      if (s1) spans[base + __popc(m1 & lt)] = make_uint4((uint32_t)c1, (uint32_t)lo, (uint32_t)split, pw | kParentLeft);
+      if (s2)
+        spans[base + __popc(m1) + __popc(m2 & lt)] = make_uint4((uint32_t)c2, (uint32_t)(split + 1), (uint32_t)hi, pw);
+    }
+  }
+  if (!act) return;
+  const uint32_t spanbit = (lo / kRefitBlock != hi / kRefitBlock) ? kParentSpans : 0u;
+  parent[c1 < 0 ? (n - 1) + split : split] = (uint32_t)i | kParentLeft | spanbit;
+  parent[c2 < 0 ? (n - 1) + split + 1 : split + 1] = (uint32_t)i | spanbit;
   // a leaf child takes one slot of this node's wide node: mark the other empty
   const float4 empty = make_float4(0.f, 0.f, 0.f, __int_as_float(kNoChild));
   if (c1 < 0) wnodes[i].s[1].lo_code = empty;
   if (c2 < 0) wnodes[i].s[3].lo_code = empty;
 }
 
-// The climb through the spanning nodes (leaf ranges over several blocks),
-// after k_refit stopped every climber at its first spanning parent and
-// recorded the arrival (its parent word; its box is in the wide node).  Each
-// arrival meets its sibling at gpu scope: a release/acquire add on the
-// parent's flag, whose parity tells the second arrival, which takes the union
-// and climbs on.  Spanning nodes have spanning parents, so every further
-// step meets the same way.  A separate launch keeps k_refit's blocks from
-// being held by a few long climbs.
-__global__ void __launch_bounds__(256) k_refit_top(WNode* wnodes, const uint32_t* __restrict__ parent,
-                                                   const uint32_t* __restrict__ arrivals, int n, int* flags,
-                                                   SceneGlobals* g) {
+// Box helpers: six floats (lo xyz, hi xyz) at 8-byte aligned addresses,
+// through L2 (written and read by different blocks).
+__device__ __forceinline__ void box_union6(float b[6], const float* q) {
+  const float2 x = __ldcg(reinterpret_cast<const float2*>(q)), y = __ldcg(reinterpret_cast<const float2*>(q) + 1),
+               z = __ldcg(reinterpret_cast<const float2*>(q) + 2);
+  b[0] = fminf(b[0], x.x), b[1] = fminf(b[1], x.y), b[2] = fminf(b[2], y.x);
+  b[3] = fmaxf(b[3], y.y), b[4] = fmaxf(b[4], z.x), b[5] = fmaxf(b[5], z.y);
+}
+__device__ __forceinline__ void box_store6(float* q, const float b[6]) {
+  float2* d = reinterpret_cast<float2*>(q);
+  __stcg(d, make_float2(b[0], b[1]));
+  __stcg(d + 1, make_float2(b[2], b[3]));
+  __stcg(d + 2, make_float2(b[4], b[5]));
+}
+
+// The boxes of the spanning nodes (leaf ranges over several refit blocks).
+// Each is the union of its leaves' boxes, and its leaf range [lo, hi] is
+// known from the split search, so no climb is needed: the box is the union
+// of the boxes of leaves lo..end of lo's block (suf[lo]), of the blocks in
+// between (suf at a block's first leaf, or gbox for whole groups of
+// kSpanGroup blocks) and of leaves start of hi's block..hi (pre[hi]), all
+// written by k_refit.  (lo
+// starts the leftmost maximal block-local node under the spanning node,
+// which is a left child of a spanning node, and hi ends the rightmost one, a
+// right child: k_refit writes suf and pre at both ends of every such node.)
+// kSpanLanes lanes per listed node share the blocks and groups in between;
+// the item after the list is the root.  min/max are exact, so the boxes
+// equal those of the reference's climb.
+constexpr int kSpanLanes = 8;
+
+__global__ void __launch_bounds__(256) k_refit_spans(WNode* wnodes, const uint32_t* __restrict__ parent,
+                                                     const uint4* __restrict__ spans, const float* suf,
+                                                     const float* pre, const int* gbox, int n, SceneGlobals* g) {
   pdl_wait();
   pdl_launch_dependents();
-  const unsigned count = *(volatile unsigned*)&g->narr;
-  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-    uint32_t w = __ldg(arrivals + i);
-    int p = (int)(w & kParentMask);
-    if (p >= n - 1) {  // only a corrupt tree gets here
-      atomicOr(&g->err, kErrStack);
-      continue;
+  const unsigned count = *(volatile unsigned*)&g->nspan;
+  const int sub = threadIdx.x & (kSpanLanes - 1);
+  const unsigned groups = (gridDim.x * blockDim.x) / kSpanLanes;
+  const unsigned first = (blockIdx.x * blockDim.x + threadIdx.x) / kSpanLanes;
+  // every lane of a warp runs the same number of rounds (the shuffles below)
+  const unsigned rounds = (count + 1 + groups - 1) / groups;
+  for (unsigned rnd = 0; rnd < rounds; rnd++) {
+    const unsigned item = first + rnd * groups;
+    const bool live = item <= count;
+    const bool root = item == count;
+    uint4 e = make_uint4(0u, 0u, (uint32_t)(n - 1), 0u);
+    if (live && !root) e = __ldg(spans + item);
+    const int lo = (int)e.y, hi = (int)e.z;
+    bool ok = live;
+    if (live && !root && ((unsigned)lo >= (unsigned)n || (unsigned)hi >= (unsigned)n ||
+                          lo / kRefitBlock >= hi / kRefitBlock)) {
+      if (sub == 0) atomicOr(&g->err, kErrStack);  // only a corrupt list gets here
+      ok = false;
     }
-    uint32_t wn = (p == 0) ? 0u : __ldg(parent + p);
-    bool is_left = (w & kParentLeft) != 0;
-    int gp = (p == 0) ? n - 1 : (int)(wn & kParentMask);
-    bool p_left = (p == 0) || (wn & kParentLeft) != 0;
-    if (p != 0 && gp >= n - 1) {
-      atomicOr(&g->err, kErrStack);
-      continue;
-    }
-    float lo[3], hi[3];
-    {
-      const WSlot* q = wnodes[gp].s + (p_left ? 0 : 2) + (is_left ? 0 : 1);
-      const float4 a = __ldcg(&q->lo_code), b = __ldcg(&q->hi);
-      lo[0] = a.x, lo[1] = a.y, lo[2] = a.z, hi[0] = b.x, hi[1] = b.y, hi[2] = b.z;
-    }
-    for (int level = 0;; level++) {
-      // the next level's parent word, fetched while this level meets
-      const uint32_t wn_next = (p == 0) ? 0u : __ldg(parent + gp);
-      if ((atomic_add_acq_rel(flags + p, 1) & 1) == 0) break;  // first arrival
-      sibling_box(wnodes, gp, p_left, is_left, lo, hi);
-      if (p == 0) {
+    // blocks strictly between the ends (the root: all): [b0, h) and [t, b1)
+    // one by one, the whole groups in [h, t) from gbox
+    const int b0 = root ? 0 : lo / kRefitBlock + 1;
+    int b1 = root ? (n - 1) / kRefitBlock + 1 : hi / kRefitBlock;
+    int h = min(b1, (b0 + kSpanGroup - 1) / kSpanGroup * kSpanGroup);
+    int t = max(h, b1 / kSpanGroup * kSpanGroup);
+    if (!ok) h = t = b1 = b0;
+    const int nh = h - b0, ng = (t - h) / kSpanGroup, nt = b1 - t, total = nh + ng + nt;
+    float b[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    for (int j = sub; j < total; j += kSpanLanes) {
+      if (j >= nh && j < nh + ng) {
+        const int* q = gbox + 6 * (size_t)(h / kSpanGroup + j - nh);
 #pragma unroll
-        for (int q = 0; q < 3; q++) g->root_box[q] = lo[q], g->root_box[3 + q] = hi[q];
-        break;
+        for (int c = 0; c < 3; c++)
+          b[c] = fminf(b[c], ord2f(__ldcg(q + c))), b[3 + c] = fmaxf(b[3 + c], ord2f(__ldcg(q + 3 + c)));
+      } else {
+        box_union6(b, suf + 6 * (size_t)kRefitBlock * (size_t)(j < nh ? b0 + j : t + j - nh - ng));
       }
-      // climb: p's box becomes a child slot one level up
-      const int xc = p;
-      w = wn;
-      p = (int)(w & kParentMask);
-      if (level >= kStackSize || p >= n - 1) {  // only a corrupt tree gets here
-        atomicOr(&g->err, kErrStack);
-        break;
-      }
-      wn = wn_next;
-      is_left = (w & kParentLeft) != 0;
-      gp = (p == 0) ? n - 1 : (int)(wn & kParentMask);
-      p_left = (p == 0) || (wn & kParentLeft) != 0;
-      if (gp >= n - 1 && p != 0) {
-        atomicOr(&g->err, kErrStack);
-        break;
-      }
-      put_wide(wnodes, xc, is_left, p, gp, p_left, lo, hi);
     }
+    if (__any_sync(0xffffffffu, total > 0)) {
+#pragma unroll
+      for (int o = kSpanLanes / 2; o > 0; o >>= 1) {
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+          b[q] = fminf(b[q], __shfl_xor_sync(0xffffffffu, b[q], o));
+          b[3 + q] = fmaxf(b[3 + q], __shfl_xor_sync(0xffffffffu, b[3 + q], o));
+        }
+      }
+    }
+    if (!ok || sub != 0) continue;
+    if (root) {
+#pragma unroll
+      for (int q = 0; q < 6; q++) g->root_box[q] = b[q];
+      continue;
+    }
+    box_union6(b, suf + 6 * (size_t)lo);
+    box_union6(b, pre + 6 * (size_t)hi);
+    const int x = (int)e.x, p = (int)(e.w & kParentMask);
+    const uint32_t wn = (p == 0) ? 0u : __ldg(parent + p);
+    const int gp = (p == 0) ? n - 1 : (int)(wn & kParentMask);
+    if (x <= 0 || x >= n - 1 || p >= n - 1 || (p != 0 && gp >= n - 1)) {  // only a corrupt tree gets here
+      atomicOr(&g->err, kErrStack);
+      continue;
+    }
+    const float lo3[3] = {b[0], b[1], b[2]}, hi3[3] = {b[3], b[4], b[5]};
+    put_wide(wnodes, x, (e.w & kParentLeft) != 0, p, gp, (p == 0) || (wn & kParentLeft) != 0, lo3, hi3);
   }
 }
 
-__global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__ V, const int* __restrict__ vidx,
+__global__ void __launch_bounds__(kRefitBlock, 4) k_refit(const float* __restrict__ V, const int* __restrict__ vidx,
                                                        const uint32_t* __restrict__ ids, int n,
                                                        WNode* wnodes, LeafTri* __restrict__ leaves,
-                                                       const uint32_t* __restrict__ parent,
-                                                       uint32_t* __restrict__ arrivals, SceneGlobals* g) {
-  __shared__ float4 s_box[kRefitBlock][2][2];  // children's boxes at each block-local node (lo, hi)
+                                                       const uint32_t* __restrict__ parent, float* __restrict__ suf,
+                                                       float* __restrict__ pre, int* __restrict__ gbox,
+                                                       SceneGlobals* g) {
+  // children's boxes at each block-local node (lo, hi); lo.w: the leaf-range
+  // end the first arrival brings (its first leaf if it is the left child,
+  // else its last)
+  __shared__ float4 s_box[kRefitBlock][2][2];
   __shared__ int s_flag[kRefitBlock];
+  // the block's maximal block-local nodes (their parents span): box, and
+  // first / last leaf in lo.w / hi.w
+  __shared__ float4 s_top[kRefitBlock][2];
+  __shared__ int s_ntop;
   s_flag[threadIdx.x] = 0;
+  if (threadIdx.x == 0) s_ntop = 0;
   pdl_wait();
   pdl_launch_dependents();
   __syncthreads();
@@ -492,29 +578,44 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__
   const int k = k0 + threadIdx.x;
   float e = 0.f;
   bool ok = true;
-  const int tri = k < n ? (int)__ldg(ids + k) : 0;
-  if (k < n && (unsigned)tri >= (unsigned)n) {  // only a corrupt sort gets here
-    atomicOr(&g->err, kErrStack);
-  } else if (k < n) {
-    float3 a, b, c;
-    float lo[3], hi[3];
-    tri_box(V, vidx, tri, a, b, c, lo, hi);
-    ok = finite_coords(a, b, c);
-    e = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
-    LeafTri lt;
-    lt.v0 = make_float4(a.x, a.y, a.z, __int_as_float(tri));
-    lt.v1 = make_float4(b.x, b.y, b.z, 0.f);
-    lt.v2 = make_float4(c.x, c.y, c.z, 0.f);
-    leaves[k] = lt;
+  int top = -1;  // this thread's entry in s_top
+  int l = k, r = k;  // leaf range of the climbing node
+  float lo[3], hi[3];
+  bool live = false;
+  if (k < n) {
+    const int tri = (int)__ldg(ids + k);
+    if ((unsigned)tri >= (unsigned)n) {  // only a corrupt sort gets here
+      atomicOr(&g->err, kErrStack);
+    } else {
+      float3 a, b, c;
+      tri_box(V, vidx, tri, a, b, c, lo, hi);
+      ok = finite_coords(a, b, c);
+      e = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+      LeafTri lt;
+      lt.v0 = make_float4(a.x, a.y, a.z, __int_as_float(tri));
+      lt.v1 = make_float4(b.x, b.y, b.z, 0.f);
+      lt.v2 = make_float4(c.x, c.y, c.z, 0.f);
+      leaves[k] = lt;
+      live = true;
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, off));
+  const bool all_ok = __all_sync(0xffffffffu, ok);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&g->emax, f2ord(e));
+    if (!all_ok) atomicOr(&g->err, kErrNonFinite);
+  }
+  if (live) {
     if (n == 1) {
 #pragma unroll
       for (int q = 0; q < 3; q++) g->root_box[q] = lo[q], g->root_box[3 + q] = hi[q];
     } else {
       uint32_t w = __ldg(parent + (n - 1) + k);
       int xc = ~k;  // code of the node that climbs (a leaf, then internal nodes)
-      for (int level = 0;; level++) {
+      for (;;) {
         const int p = (int)(w & kParentMask);
-        if (level >= kStackSize || p >= n - 1) {  // only a corrupt tree gets here
+        if (p >= n - 1) {  // only a corrupt tree gets here
           atomicOr(&g->err, kErrStack);
           break;
         }
@@ -529,19 +630,36 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__
         put_wide(wnodes, xc, is_left, p, gp, p_left, lo, hi);
         if (!(w & kParentSpans)) {  // both arrivals are threads of this block
           const int sl = p - k0;
+          if ((unsigned)sl >= (unsigned)kRefitBlock) {  // only a corrupt tree gets here
+            atomicOr(&g->err, kErrStack);
+            break;
+          }
           float4* mine = s_box[sl][is_left ? 0 : 1];
-          mine[0] = make_float4(lo[0], lo[1], lo[2], 0.f);
+          mine[0] = make_float4(lo[0], lo[1], lo[2], __int_as_float(is_left ? l : r));
           mine[1] = make_float4(hi[0], hi[1], hi[2], 0.f);
           __threadfence_block();
-          if (atomicAdd(&s_flag[sl], 1) == 0) break;  // first arrival
+          // the first arrival stops; only the second climbs on (so a corrupt
+          // tree cannot make a climb loop: each slot lets one climber through)
+          const int arrived = atomicAdd(&s_flag[sl], 1);
+          if (arrived != 1) {
+            if (arrived != 0) atomicOr(&g->err, kErrStack);
+            break;
+          }
           __threadfence_block();
           const float4* o = s_box[sl][is_left ? 1 : 0];
           const float4 ol = o[0], oh = o[1];
           lo[0] = fminf(lo[0], ol.x), lo[1] = fminf(lo[1], ol.y), lo[2] = fminf(lo[2], ol.z);
           hi[0] = fmaxf(hi[0], oh.x), hi[1] = fmaxf(hi[1], oh.y), hi[2] = fmaxf(hi[2], oh.z);
+          if (is_left)
+            r = __float_as_int(ol.w);
+          else
+            l = __float_as_int(ol.w);
         } else {
-          // spanning node: its climb continues in k_refit_top (its box is in the wide node)
-          arrivals[atomicAdd(&g->narr, 1u)] = w;
+          // the parent spans: k_refit_spans finds its box from the block boxes
+          // and the edge boxes written below
+          top = atomicAdd(&s_ntop, 1);
+          s_top[top][0] = make_float4(lo[0], lo[1], lo[2], __int_as_float(l));
+          s_top[top][1] = make_float4(hi[0], hi[1], hi[2], __int_as_float(r));
           break;
         }
         if (p == 0) {
@@ -554,20 +672,42 @@ __global__ void __launch_bounds__(kRefitBlock) k_refit(const float* __restrict__
       }
     }
   }
+  // The maximal block-local nodes tile the block's leaves.  Each writes the
+  // union of its own and the later ones' boxes at its first leaf (suf) and of
+  // the earlier ones' and its own at its last leaf (pre).
+  __syncthreads();
+  const int ntop = s_ntop;
+  if (top >= 0) {
+    const int l = __float_as_int(s_top[top][0].w), r = __float_as_int(s_top[top][1].w);
+    // one pass per edge box keeps the live registers down
+    for (int side = 0; side < 2; side++) {
+      float u[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+      for (int t = 0; t < ntop; t++) {
+        const float4 a = s_top[t][0], b = s_top[t][1];
+        if (side == 0 ? __float_as_int(a.w) >= l : __float_as_int(b.w) <= r) {
+          u[0] = fminf(u[0], a.x), u[1] = fminf(u[1], a.y), u[2] = fminf(u[2], a.z);
+          u[3] = fmaxf(u[3], b.x), u[4] = fmaxf(u[4], b.y), u[5] = fmaxf(u[5], b.z);
+        }
+      }
+      box_store6(side == 0 ? suf + 6 * (size_t)l : pre + 6 * (size_t)r, u);
+      if (side == 0 && l == k0) {
+        // suf at the block's first leaf is the block's box; it also joins
+        // the box of the block's group of kSpanGroup blocks, by exact atomic
+        // min/max on order-preserving integers (reset before every refit)
+        int* q = gbox + 6 * (blockIdx.x / kSpanGroup);
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) e = fmaxf(e, __shfl_xor_sync(0xffffffffu, e, off));
-  const bool all_ok = __all_sync(0xffffffffu, ok);
-  if ((threadIdx.x & 31) == 0) {
-    atomicMax(&g->emax, f2ord(e));
-    if (!all_ok) atomicOr(&g->err, kErrNonFinite);
+        for (int c = 0; c < 3; c++) atomicMin(q + c, f2ord(u[c])), atomicMax(q + 3 + c, f2ord(u[3 + c]));
+      }
+    }
   }
 }
 
 }  // namespace
 
 namespace {
-__global__ void k_refit_init(SceneGlobals* g) {
-  if (threadIdx.x == 0) g->emax = f2ord(0.f), g->narr = 0u;
+__global__ void k_refit_init(SceneGlobals* g, int* gbox, int groups) {
+  if (threadIdx.x == 0) g->emax = f2ord(0.f);
+  clear_group_boxes(gbox, groups);
 }
 }  // namespace
 
@@ -622,11 +762,11 @@ static void onesweep_pass(const uint32_t* kin, const uint32_t* vin, uint32_t* ko
 static void refit(const MeshBufs& m, const BuildBufs& b, cudaStream_t st) {
   const int n = m.ntri;
   launch_k(true, k_refit, (n + kRefitBlock - 1) / kRefitBlock, kRefitBlock, st, (const float*)m.verts,
-           (const int*)m.vidx, (const uint32_t*)b.vals_b, n, b.wnodes, b.leaves, (const uint32_t*)b.parent,
-           b.arrivals, b.g);
+           (const int*)m.vidx, (const uint32_t*)b.vals_b, n, b.wnodes, b.leaves, (const uint32_t*)b.parent, b.suf,
+           b.pre, b.gbox, b.g);
   if (n > kRefitBlock)
-    launch_k(true, k_refit_top, num_sms() * 2, 256, st, b.wnodes, (const uint32_t*)b.parent,
-             (const uint32_t*)b.arrivals, n, b.flags, b.g);
+    launch_k(true, k_refit_spans, num_sms() * 8, 256, st, b.wnodes, (const uint32_t*)b.parent,
+             (const uint4*)b.spans, (const float*)b.suf, (const float*)b.pre, (const int*)b.gbox, n, b.g);
 }
 
 // Whether the build's sort runs as one cooperative launch (k_sort_coop): its
@@ -651,14 +791,18 @@ cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st)
   const int passes = 3;
   const int tiles = sort_tiles(n);
   const bool coop = coop_sort_fits(n);
-  k_build_init<<<1, 1024, 0, st>>>(b.g, b.hist, passes * kRadix);
+  k_build_init<<<1, 1024, 0, st>>>(b.g, b.hist, passes * kRadix, b.gbox, (int)span_groups(n));
   const int sms = num_sms();
   const int gb = min((n + 255) / 256, sms * 8);
   launch_k(true, k_bounds, gb, 256, st, (const float*)m.verts, (const int*)m.vidx, n, b.g);
   const int gm = min((n + 511) / 512, sms * 2);
   // (the look-back status is cleared only for the passes that use it)
-  launch_k(true, k_morton, gm, 512, st, (const float*)m.verts, (const int*)m.vidx, n, (const SceneGlobals*)b.g,
-           b.keys_a, b.hist, passes, b.status, coop ? 0 : passes * tiles * kRadix);
+  if (coop)
+    launch_k(true, k_morton<false>, gm, 512, st, (const float*)m.verts, (const int*)m.vidx, n,
+             (const SceneGlobals*)b.g, b.keys_a, b.hist, passes, b.status, 0);
+  else
+    launch_k(true, k_morton<true>, gm, 512, st, (const float*)m.verts, (const int*)m.vidx, n,
+             (const SceneGlobals*)b.g, b.keys_a, b.hist, passes, b.status, passes * tiles * kRadix);
   // pass 0: keys_a -> keys_b (values 0..n-1), pass 1: b -> a, pass 2: a -> b
   if (coop) {
     cudaLaunchConfig_t cfg = {};
@@ -672,7 +816,7 @@ cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st)
     cfg.numAttrs = 1;
     // barrier words: tile_counter[0..1], zeroed by k_build_init
     cudaLaunchKernelEx(&cfg, k_sort_coop<kSortThreadsL, kSortItems>, b.keys_a, b.keys_b, b.vals_a, b.vals_b, n,
-                       passes, (const uint32_t*)b.hist, b.status, &b.g->tile_counter[0], &b.g->err);
+                       passes, b.status, &b.g->tile_counter[0], &b.g->err);
   } else {
     const uint32_t* kin = b.keys_a;
     const uint32_t* vin = nullptr;
@@ -687,7 +831,7 @@ cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st)
   }
   if (n >= 2)
     launch_k(true, k_hierarchy, (n - 1 + kHierThreads - 1) / kHierThreads, kHierThreads, st,
-             (const uint32_t*)b.keys_b, n, b.parent, b.flags, b.wnodes);
+             (const uint32_t*)b.keys_b, n, b.parent, b.wnodes, b.spans, &b.g->nspan);
   refit(m, b, st);
   return cudaGetLastError();
 }
@@ -716,10 +860,11 @@ __global__ void __launch_bounds__(256) k_nodes3(const uint32_t* __restrict__ par
 }
 
 cudaError_t launch_stage_hierarchy(const uint32_t* codes, const uint32_t* ids, int n, int* nodes3,
-                                   uint32_t* parent, int* flags, WNode* wnodes, cudaStream_t st) {
+                                   uint32_t* parent, WNode* wnodes, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   if (n >= 2)
-    k_hierarchy<<<(n - 1 + kHierThreads - 1) / kHierThreads, kHierThreads, 0, st>>>(codes, n, parent, flags, wnodes);
+    k_hierarchy<<<(n - 1 + kHierThreads - 1) / kHierThreads, kHierThreads, 0, st>>>(codes, n, parent, wnodes,
+                                                                                     nullptr, nullptr);
   k_nodes3<<<(2 * n - 1 + 255) / 256, 256, 0, st>>>(parent, ids, n, nodes3);
   return cudaGetLastError();
 }
@@ -811,7 +956,7 @@ cudaError_t launch_check_indices(const MeshBufs& m, const BuildBufs& b, cudaStre
 cudaError_t launch_refit(const MeshBufs& m, const BuildBufs& b, cudaStream_t st) {
   const int n = m.ntri;
   if (n <= 0) return cudaSuccess;
-  k_refit_init<<<1, 32, 0, st>>>(b.g);
+  k_refit_init<<<1, 256, 0, st>>>(b.g, b.gbox, (int)span_groups(n));
   refit(m, b, st);
   return cudaGetLastError();
 }

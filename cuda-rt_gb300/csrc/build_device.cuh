@@ -88,33 +88,57 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
+// Per-axis constants of morton_cell for a scene box [mn, mx]: the extent
+// mx - mn as an exact float-float pair (dh, dl), and 1/dh rounded to nearest
+// and upwards.  `fast` is false when dh is not positive or lies outside
+// [2^-125, 2^125] (the reciprocals are then not normal floats): every cell of
+// that axis comes from the double path.
+struct MortonAxis {
+  float mn, mx, dh, dl, rcp, rcp_up;
+  bool fast;
+};
+__device__ __forceinline__ MortonAxis morton_axis_setup(float mn, float mx) {
+  MortonAxis a;
+  a.mn = mn;
+  a.mx = mx;
+  two_sum(mx, -mn, a.dh, a.dl);
+  a.fast = a.dh >= 2.3509887e-38f && a.dh <= 4.2535296e37f;  // 2^-125, 2^125
+  a.rcp = __frcp_rn(a.dh);
+  a.rcp_up = __frcp_ru(a.dh);
+  return a;
+}
+
 // The same cell without double arithmetic whenever that is provably right.
 // y = 1024 (c - mn) / (mx - mn) is formed in float-float: c = (lo + hi)/2,
-// c - mn and mx - mn by exact two-sums, then one division with an FMA-based
-// correction, so y_hi + y_lo is within E = 2^-30 (|y| + 1024 (|c| + |mn|)/den)
-// of the exact quotient (about 2^10 over a first-order bound; the double path's
-// own error is smaller still).  The cell is floor(y) unless y sits within half
-// a float ulp (<= 2^-15 below 1024) of the next integer, or the bound does not
-// separate y from an integer: then the double path decides.
-__device__ __forceinline__ uint32_t morton_cell(float lo, float hi, float mn, float mx) {
-  float dh, dl;
-  two_sum(mx, -mn, dh, dl);
-  if (dh > 0.f) {
+// c - mn and mx - mn by exact two-sums, then a quotient q1 = nh * RN(1/dh)
+// and one correction term from the exact residual (q1*dh split by an FMA).
+// q1 is within 2^-23 of nh/dh (relative), the computed residual within
+// ~2^-45 |nh|, so y_hi + y_lo is within ~2^-34 |nh| / dh of the exact
+// quotient -- far inside E = 2^-30 (|y| + 1024 (|c| + |mn|)/dh), the bound
+// the checks below use (|nh| <= |c| + |mn|).  E is evaluated with upward
+// rounding and the upward reciprocal, so it never falls below that value.
+// The cell is floor(y) unless y sits within half a float ulp (<= 2^-15 below
+// 1024) of the next integer, or the bound does not separate y from an
+// integer: then the double path decides.  Any overflow or NaN fails every
+// check and also goes to the double path.
+__device__ __forceinline__ uint32_t morton_cell(float lo, float hi, const MortonAxis& ax) {
+  if (ax.fast) {
+    const float mn = ax.mn, dh = ax.dh, dl = ax.dl;
     float sh, sl;
     two_sum(lo, hi, sh, sl);
     const float ch = 0.5f * sh, cl = 0.5f * sl;  // exact halving
     float nh, nl;
     two_sum(ch, -mn, nh, nl);
     nl = __fadd_rn(nl, cl);
-    const float q1 = __fdiv_rn(nh, dh);
+    const float q1 = __fmul_rn(nh, ax.rcp);
     // r = (nh + nl) - q1 (dh + dl), with q1*dh split exactly by an FMA
     const float ph = __fmul_rn(q1, dh);
     const float pl = __fmaf_rn(q1, dh, -ph);
     const float r = __fadd_rn(__fsub_rn(__fsub_rn(nh, ph), pl), __fsub_rn(nl, __fmul_rn(q1, dl)));
-    const float q2 = __fdiv_rn(r, dh);
+    const float q2 = __fmul_rn(r, ax.rcp);
     const float yh = 1024.f * q1, yl = 1024.f * q2;  // exact scaling
-    const float E = __fmul_ru(9.3132257e-10f, __fadd_ru(fabsf(yh), __fmul_ru(1024.f, __fdiv_ru(__fadd_ru(fabsf(ch),
-                                                                                                   fabsf(mn)), dh))));
+    const float E = __fmul_ru(9.3132257e-10f, __fadd_ru(fabsf(yh), __fmul_ru(1024.f, __fmul_ru(__fadd_ru(fabsf(ch),
+                                                                                                   fabsf(mn)), ax.rcp_up))));
     if (__fadd_ru(__fadd_ru(yh, yl), E) < 0.f) return 0u;
     if (__fsub_rd(__fsub_rd(yh, -yl), E) > 1023.f) return 1023u;
     const float fl = floorf(yh);
@@ -125,23 +149,19 @@ __device__ __forceinline__ uint32_t morton_cell(float lo, float hi, float mn, fl
         return (uint32_t)fl;
     }
   }
-  return morton_axis_exact(lo, hi, (double)mn, (double)mx);
+  return morton_axis_exact(lo, hi, (double)ax.mn, (double)ax.mx);
 }
 
-__device__ __forceinline__ uint32_t morton_code(const float lo[3], const float hi[3], const float mn[3],
-                                                const float mx[3]) {
-  const uint32_t ex = expand_bits(morton_cell(lo[0], hi[0], mn[0], mx[0]));
-  const uint32_t ey = expand_bits(morton_cell(lo[1], hi[1], mn[1], mx[1]));
-  const uint32_t ez = expand_bits(morton_cell(lo[2], hi[2], mn[2], mx[2]));
+__device__ __forceinline__ uint32_t morton_code(const float lo[3], const float hi[3], const MortonAxis ax[3]) {
+  const uint32_t ex = expand_bits(morton_cell(lo[0], hi[0], ax[0]));
+  const uint32_t ey = expand_bits(morton_cell(lo[1], hi[1], ax[1]));
+  const uint32_t ez = expand_bits(morton_cell(lo[2], hi[2], ax[2]));
   return ex * 4 + ey * 2 + ez;
 }
 
-__device__ __forceinline__ void load_scene_box(const SceneGlobals* g, float mn[3], float mx[3]) {
+__device__ __forceinline__ void load_scene_box(const SceneGlobals* g, MortonAxis ax[3]) {
 #pragma unroll
-  for (int k = 0; k < 3; k++) {
-    mn[k] = ord2f(g->bmin[k]);
-    mx[k] = ord2f(g->bmax[k]);
-  }
+  for (int k = 0; k < 3; k++) ax[k] = morton_axis_setup(ord2f(g->bmin[k]), ord2f(g->bmax[k]));
 }
 
 __device__ __forceinline__ int atomic_add_acq_rel(int* p, int v) {
@@ -185,6 +205,29 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_warp
   __syncthreads();
   total = tot;
   return wpre + x - v;
+}
+
+// The same for two values per thread at once (a, b < 2^32 in total over the
+// block): returns both exclusive prefixes.
+template <int TH>
+__device__ __forceinline__ void block_excl_scan2(uint32_t a, uint32_t b, unsigned long long* s_warp, uint32_t& pa,
+                                                 uint32_t& pb) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned long long v = ((unsigned long long)a << 32) | b;
+  unsigned long long x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  unsigned long long wpre = 0;
+  for (int w = 0; w < warp; w++) wpre += s_warp[w];
+  __syncthreads();
+  const unsigned long long r = wpre + x - v;
+  pa = (uint32_t)(r >> 32);
+  pb = (uint32_t)r;
 }
 
 constexpr uint32_t kFlagAgg = 1u << 30, kFlagInc = 2u << 30, kValMask = (1u << 30) - 1;
@@ -272,6 +315,7 @@ struct SortSmem {
   uint32_t keys[STAGE ? TH * IT : 1];
   uint32_t vals[STAGE ? TH * IT : 1];
   uint32_t warp[TH / 32];
+  unsigned long long warp2[TH / 32];
   int tile;
 };
 
@@ -471,8 +515,8 @@ __device__ __forceinline__ int kdelta(const uint32_t* __restrict__ c, int n, uin
 
 // The parent word of a node: parent index | bit 31 when the node is its
 // parent's left child | bit 30 when the parent's leaf range crosses a
-// kRefitBlock boundary (the refit then meets at gpu scope).
-constexpr int kRefitBlock = 512;
+// kRefitBlock boundary (a spanning node: its box does not come from the
+// block-local climbs).
 constexpr uint32_t kParentLeft = 1u << 31, kParentSpans = 1u << 30, kParentMask = (1u << 30) - 1;
 
 // The largest m in [0, limit] with pred(m), for a predicate true on a prefix
@@ -507,12 +551,14 @@ __device__ __forceinline__ int warp_prefix_end(int limit, Pred pred) {
 // A block owns kRefitBlock consecutive sorted leaves.  A node whose leaf
 // range lies inside that span has both children's climbers in the block, so
 // its two arrivals meet in shared memory with block-scope ordering (most
-// nodes).  A node spanning several blocks uses the global flag with
-// release/acquire at gpu scope and reads its other child's box from the wide
-// node.  Global flags count arrivals; each refit adds exactly two per
-// spanning node, so the parity of the old value tells first from second
-// without clearing between refits.  Each climb step needs one dependent load:
-// the parent word (index, side, spanning bit).
+// nodes).  The single-scene build (k_refit_spans) then takes each node
+// spanning several blocks as the union of block and block-edge boxes; the
+// batched build meets there too, through a global flag with release/acquire
+// at gpu scope, reading the other child's box from the wide node (global
+// flags count arrivals; each refit adds exactly two per spanning node, so the
+// parity of the old value tells first from second without clearing between
+// refits).  Each climb step needs one dependent load: the parent word (index,
+// side, spanning bit).
 __device__ __forceinline__ void put_wide(WNode* W, int xc, bool x_left, int p, int gp, bool p_left,
                                          const float lo[3], const float hi[3]) {
   const float4 a = make_float4(lo[0], lo[1], lo[2], __int_as_float(xc));

@@ -226,12 +226,13 @@ static crt_status create_scene(const crt_mesh_desc* d, void* stream, bool borrow
   b.n = n;
   const int tiles = sort_tiles(n > 0 ? n : 1);
   const size_t nn = n > 0 ? 2 * (size_t)n - 1 : 0;
-  size_t off[11], total = 0;
-  const size_t sizes[11] = {4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n, 4 * 3 * (size_t)kRadix,
-                            4 * 3 * (size_t)tiles * kRadix, 4 * nn, 4 * (size_t)(n > 1 ? n - 1 : 1),
-                            4 * (size_t)(n > 0 ? n : 1), sizeof(LeafTri) * (size_t)(n > 0 ? n : 1),
-                            sizeof(WNode) * (size_t)(n > 0 ? n : 1)};
-  for (int i = 0; i < 11; i++) off[i] = total, total += align256(sizes[i]);
+  const size_t n1 = n > 0 ? (size_t)n : 1;
+  size_t off[13], total = 0;
+  const size_t sizes[13] = {4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n, 4 * (size_t)n, 4 * 3 * (size_t)kRadix,
+                            4 * 3 * (size_t)tiles * kRadix, 4 * nn, sizeof(uint4) * n1,
+                            sizeof(float) * 6 * n1, sizeof(float) * 6 * n1, sizeof(int) * 6 * span_groups(n),
+                            sizeof(LeafTri) * n1, sizeof(WNode) * n1};
+  for (int i = 0; i < 13; i++) off[i] = total, total += align256(sizes[i]);
   const size_t goff = total;
   total += align256(sizeof(SceneGlobals));
   ALLOC(s->block, total);
@@ -245,13 +246,14 @@ static crt_status create_scene(const crt_mesh_desc* d, void* stream, bool borrow
   b.hist = reinterpret_cast<uint32_t*>(base + off[4]);
   b.status = reinterpret_cast<uint32_t*>(base + off[5]);
   b.parent = reinterpret_cast<uint32_t*>(base + off[6]);
-  b.flags = reinterpret_cast<int*>(base + off[7]);
-  b.arrivals = reinterpret_cast<uint32_t*>(base + off[8]);
-  b.leaves = reinterpret_cast<LeafTri*>(base + off[9]);
-  b.wnodes = reinterpret_cast<WNode*>(base + off[10]);
+  b.spans = reinterpret_cast<uint4*>(base + off[7]);
+  b.suf = reinterpret_cast<float*>(base + off[8]);
+  b.pre = reinterpret_cast<float*>(base + off[9]);
+  b.gbox = reinterpret_cast<int*>(base + off[10]);
+  b.leaves = reinterpret_cast<LeafTri*>(base + off[11]);
+  b.wnodes = reinterpret_cast<WNode*>(base + off[12]);
   b.g = reinterpret_cast<SceneGlobals*>(base + goff);
   if ((e = cudaMemsetAsync(b.g, 0, sizeof(SceneGlobals), st)) != cudaSuccess) return bail(e, "memset");
-  if ((e = cudaMemsetAsync(b.flags, 0, sizes[7], st)) != cudaSuccess) return bail(e, "memset");
   // upload
   auto up = [&](void* dst, const void* src, size_t bytes) {
     return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, st) : cudaSuccess;
@@ -654,13 +656,12 @@ crt_status crt_hierarchy(const uint32_t* codes, const uint32_t* ids, int32_t n, 
     return fail(CRT_INVALID_ARG, "crt_hierarchy takes device pointers");
   cudaStream_t st = S(stream);
   const size_t nn = 2 * (size_t)n - 1;
-  const size_t bytes = align256(4 * nn) + align256(4 * (size_t)n) + sizeof(WNode) * (size_t)n;
+  const size_t bytes = align256(4 * nn) + sizeof(WNode) * (size_t)n;
   char* scratch = nullptr;
   CRT_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scratch), bytes, st), "scratch");
   uint32_t* parent = reinterpret_cast<uint32_t*>(scratch);
-  int* flags = reinterpret_cast<int*>(scratch + align256(4 * nn));
-  WNode* wnodes = reinterpret_cast<WNode*>(scratch + align256(4 * nn) + align256(4 * (size_t)n));
-  const cudaError_t e = launch_stage_hierarchy(codes, ids, n, nodes3, parent, flags, wnodes, st);
+  WNode* wnodes = reinterpret_cast<WNode*>(scratch + align256(4 * nn));
+  const cudaError_t e = launch_stage_hierarchy(codes, ids, n, nodes3, parent, wnodes, st);
   CRT_CUDA(cudaFreeAsync(scratch, st), "free");
   CRT_CUDA(e, "hierarchy launch");
   return CRT_OK;

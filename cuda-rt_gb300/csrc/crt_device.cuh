@@ -61,7 +61,7 @@ struct SceneGlobals {
   int emax;              // largest per-axis extent of a triangle box (encoded)
   int err;               // CRT_ERR_* bits
   unsigned tile_counter[4];
-  unsigned narr;         // climbs the refit hands to its spanning-node pass
+  unsigned nspan;        // spanning internal nodes listed by the split search
   float root_box[6];     // box of the root (lo xyz, hi xyz)
 };
 

@@ -24,6 +24,14 @@ constexpr int kSortTileL = kSortThreadsL * kSortItems;
 inline bool sort_large(int n) { return n >= (1 << 19); }
 inline int sort_tiles_used(int n) { return sort_large(n) ? (n + kSortTileL - 1) / kSortTileL : sort_tiles(n); }
 
+// Leaves per block of the refit (a node whose leaf range crosses a multiple
+// of it is a spanning node).
+constexpr int kRefitBlock = 512;
+// Refit blocks per group (the spanning-node pass reads a whole group's box at once).
+constexpr int kSpanGroup = 32;
+inline size_t refit_blocks(int n) { return n > 0 ? ((size_t)n + kRefitBlock - 1) / kRefitBlock : 1; }
+inline size_t span_groups(int n) { return (refit_blocks(n) + kSpanGroup - 1) / kSpanGroup; }
+
 // Device arrays of one scene's BVH build (owned by the scene).
 struct BuildBufs {
   int n = 0;
@@ -31,8 +39,11 @@ struct BuildBufs {
   uint32_t* hist = nullptr;    // 3 * kRadix
   uint32_t* status = nullptr;  // 3 * tiles * kRadix
   uint32_t* parent = nullptr;  // 2n - 1: parent index (reference numbering) | left-child and spanning bits
-  int* flags = nullptr;        // n - 1
-  uint32_t* arrivals = nullptr;  // n: climbs handed from the refit to its spanning-node pass
+  uint4* spans = nullptr;      // n: the spanning internal nodes (node, first leaf, last leaf, parent word)
+  float* suf = nullptr;        // 6n: box of leaves i..end of i's refit block (at first leaves of block tops;
+                               // at a block's first leaf: the block's box)
+  float* pre = nullptr;        // 6n: box of leaves start of i's refit block..i (at last leaves of block tops)
+  int* gbox = nullptr;         // 6 per group of kSpanGroup refit blocks: the group's box (order-preserving ints)
   WNode* wnodes = nullptr;     // n (the last one virtual: the root's children)
   LeafTri* leaves = nullptr;   // n
   SceneGlobals* g = nullptr;
@@ -75,9 +86,10 @@ int num_sms();
 cudaError_t launch_build(const MeshBufs& m, const BuildBufs& b, cudaStream_t st);
 cudaError_t launch_refit(const MeshBufs& m, const BuildBufs& b, cudaStream_t st);
 // Stage-level hierarchy and refit in the reference's HNode layout (scratch:
-// parent 2n - 1 words, flags n - 1, wnodes n; flags zeroed by the caller).
+// parent 2n - 1 words and wnodes n for the hierarchy; for the refit, flags
+// n - 1 zeroed by the caller).
 cudaError_t launch_stage_hierarchy(const uint32_t* codes, const uint32_t* ids, int n, int* nodes3,
-                                   uint32_t* parent, int* flags, WNode* wnodes, cudaStream_t st);
+                                   uint32_t* parent, WNode* wnodes, cudaStream_t st);
 cudaError_t launch_stage_refit(const float* V, int nv, const int* vidx, int n, const uint32_t* ids,
                                const int* nodes3, float* boxes, int* flags, int* err, cudaStream_t st);
 // Range checks of device-resident index arrays (kErrIndex in b.g->err).

@@ -121,6 +121,59 @@ def test_morton_stage_matches_oracle(cuda):
     assert_equal(codes.cpu().numpy(), want, "codes beside the bad triangles")
 
 
+def _boundary_mesh(seed):
+    """Triangles whose centroids sit on, and a few float steps either side of,
+    every Morton cell boundary of each axis (the cases the FP32 fast path must
+    hand to the double path), inside a box fixed by one frame triangle."""
+    from crt import data
+    rng = np.random.default_rng(seed)
+    mn = np.array([-3.7, 0.1, -1e-3], np.float32)
+    mx = np.array([5.3, 0.7, 2.0e3], np.float32)
+    cand = []
+    for a in range(3):
+        t = mn[a].astype(np.float64) + np.arange(1025) / 1024.0 * (mx[a].astype(np.float64) - mn[a])
+        f = t.astype(np.float32)
+        vals = [f]
+        for _ in range(3):
+            vals.append(np.nextafter(vals[-1], np.float32(np.inf)))
+        lo = f
+        for _ in range(3):
+            lo = np.nextafter(lo, np.float32(-np.inf))
+            vals.append(lo)
+        c = np.clip(np.concatenate(vals), mn[a], mx[a])
+        cand.append(c)
+    n = 60000
+    p = np.stack([cand[a][rng.integers(0, cand[a].size, n)] for a in range(3)], 1)
+    # half degenerate (centroid = the point), half with vertices a few ulps
+    # apart so that lo + hi is not a float
+    d = rng.integers(1, 4, (n, 3)).astype(np.float32) * np.spacing(np.abs(p).astype(np.float32) + 1e-30)
+    d[: n // 2] = 0
+    tri = np.stack([p - d, p + d, p], 1).astype(np.float32)
+    tri = np.clip(tri, mn, mx)
+    frame = np.stack([mn, mx, mn])[None]
+    v = np.concatenate([frame, tri]).reshape(-1, 3).astype(np.float32)
+    nt = n + 1
+    vidx = np.arange(3 * nt, dtype=np.int32).reshape(nt, 3)
+    nrm = np.tile(np.array([[0, 0, 1]], np.float32), (3 * nt, 1))
+    return data.Mesh(v, vidx, nrm, vidx.copy(), np.zeros(nt, np.int32), data.lambert_material()[None])
+
+
+def test_morton_cell_boundaries(cuda):
+    """Morton codes of centroids on and beside every cell boundary: the FP32
+    fast path either gets the double formula's cell or defers to it."""
+    import crt
+    from oracle.oracle import OracleScene
+    torch = cuda
+    m = _boundary_mesh(7)
+    ex = OracleScene(m).export()
+    box = torch.tensor(np.concatenate([ex["smin"], ex["smax"]]).astype(np.float32)).cuda()
+    codes = torch.empty(m.ntri, dtype=torch.int32, device="cuda")
+    crt.morton(torch.from_numpy(m.verts).cuda(), torch.from_numpy(m.vidx).cuda(), box, codes)
+    torch.cuda.synchronize()
+    assert_equal(codes.cpu().numpy(), ex["codes_unsorted"], "codes")
+    _build_equal(crt.Scene(m).export(), ex)
+
+
 @pytest.mark.parametrize("n", [1, 2, 3, 1000, 2049, 20000])
 def test_stage_hierarchy_and_refit(cuda, n):
     """crt_hierarchy and crt_refit, the stage-level entry points, on the
