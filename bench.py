@@ -51,8 +51,8 @@ W, H, SPP = 1920, 1080, 16
 # lines) and the threads' local memory (traversal stacks and register spills
 # of 175,104 resident threads).  Re-captured whenever those kernels change.
 RENDER_DRAM_BYTES = 12_201_627_136
-BUILD_DRAM_BYTES = 225_798_912
-BUILD_L2_BYTES = 879_124_640
+BUILD_DRAM_BYTES = 227_666_176
+BUILD_L2_BYTES = 869_048_800
 TRAFFIC_SOURCE = "ncu 2025.3 single-pass captures, GB300, 2026-12-04"
 
 

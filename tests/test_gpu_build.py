@@ -25,7 +25,9 @@ def test_build_matches_reference_golden(cuda, path):
     _build_equal(s.export(), z)
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 4, 31, 2047, 2048, 2049, 100_000])
+# 512-leaf refit blocks and groups of 32 blocks (16384 leaves): sizes at and
+# beside both edges, and a partial last group
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 31, 511, 512, 513, 2047, 2048, 2049, 16383, 16384, 16385, 16897, 100_000])
 def test_build_matches_oracle_soup(cuda, n):
     import crt
     from crt import data
