@@ -19,10 +19,13 @@ Recipe (run from this container, where the reference checkout exists):
   * kernels/scene.cu without lines 4-6 (thrust includes) and 48-85
     (Scene_d::computeBoundingBoxes, AverageSuperSampling, findMinMax: launch
     wrappers and the thrust reduction, restated in harness.cpp).
-The kept line ranges are written to oracle/_ref/src/ (git-ignored build
-intermediates, never committed) and compiled with
-``-O2 -ffp-contract=off -fopenmp`` so the double arithmetic is evaluated
-exactly as written (no FMA contraction), as in the oracle.
+The kept line ranges are written to oracle/_ref/src/ and the checkout's
+headers (inc/) to oracle/_ref/inc/ (git-ignored build intermediates, never
+committed) and compiled with ``-O2 -ffp-contract=off -fopenmp`` so the double
+arithmetic is evaluated exactly as written (no FMA contraction), as in the
+oracle.  Where no checkout exists but those intermediates do (a machine that
+received this tree with its build directory, e.g. an Arm GPU host, where the
+x86 objects are of no use), ``build_extracted`` compiles them again.
 
 Usage: python oracle/ref/build_ref.py [--reference DIR]
 """
@@ -77,6 +80,21 @@ def extract(ref, rel, ranges):
     return dst
 
 
+def copy_headers(ref):
+    dst = os.path.join(OUT, "inc")
+    os.makedirs(dst, exist_ok=True)
+    for name in sorted(os.listdir(os.path.join(ref, "inc"))):
+        with open(os.path.join(ref, "inc", name), "rb") as f:
+            data = f.read()
+        with open(os.path.join(dst, name), "wb") as f:
+            f.write(data)
+
+
+def extracted_sources():
+    srcs = [os.path.join(OUT, "src", os.path.basename(rel).replace(".cu", "_ref.cpp")) for rel, _ in PIECES]
+    return srcs if all(os.path.exists(p) for p in srcs) and os.path.isdir(os.path.join(OUT, "inc")) else None
+
+
 def build(ref=None, quiet=False):
     ref = ref or default_reference()
     if not os.path.isdir(os.path.join(ref, "kernels")):
@@ -85,11 +103,26 @@ def build(ref=None, quiet=False):
         return None
     os.makedirs(os.path.join(OUT, "src"), exist_ok=True)
     srcs = [extract(ref, rel, ranges) for rel, ranges in PIECES]
-    srcs.append(os.path.join(HERE, "harness.cpp"))
+    copy_headers(ref)
+    return _compile(srcs, quiet)
+
+
+def build_extracted(quiet=False):
+    """Compile the intermediates a build from a checkout left in oracle/_ref/."""
+    srcs = extracted_sources()
+    if srcs is None:
+        if not quiet:
+            print("build_ref: no extracted reference sources; skipped")
+        return None
+    return _compile(srcs, quiet)
+
+
+def _compile(srcs, quiet):
+    srcs = list(srcs) + [os.path.join(HERE, "harness.cpp")]
     cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
     flags = ["-std=c++17", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-w",
              "-include", os.path.join(HERE, "shim.h"),
-             "-I", os.path.join(ref, "inc"), "-I", os.path.join(ref, "kernels"), "-I", cuda_inc]
+             "-I", os.path.join(OUT, "inc"), "-I", os.path.join(OUT, "src"), "-I", cuda_inc]
     objs, procs = [], []
     for src in srcs:
         obj = os.path.join(OUT, os.path.basename(src) + ".o")
