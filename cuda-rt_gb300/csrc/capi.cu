@@ -220,7 +220,7 @@ static crt_status create_scene(const crt_mesh_desc* d, void* stream, bool borrow
     ALLOC(m.matid, sizeof(int) * (size_t)n);
     ALLOC(m.mats, sizeof(DMat) * (size_t)m.nmat);
   }
-  ALLOC(s->counter, sizeof(unsigned) * 4);
+  ALLOC(s->counter, sizeof(unsigned) * kMaxTileRegions);
   // build arrays, one block
   BuildBufs& b = s->b;
   b.n = n;

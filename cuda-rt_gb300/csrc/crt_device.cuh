@@ -606,6 +606,43 @@ __device__ __forceinline__ D3 hit_normal(const DScene& S, const HitRec& h) {
   return normalize_exact(N);
 }
 
+// ---------------------------------------------------------------- pixel tiles
+// The next tile for the calling warp (one lane calls it), or -1 when every
+// tile is taken.  The warp starts in its SM's rectangle r (home set); once
+// that is exhausted it helps the lowest-numbered rectangle that may still
+// have tiles: counters[R] holds a bound below which every rectangle is
+// exhausted, raised by the warps that find one so, so that a warp looking
+// for work skips what others have found empty.  Tiles inside a rectangle go
+// row by row; each is handed out exactly once.
+__device__ __forceinline__ int claim_tile(unsigned* counters, int tiles_x, int tiles_y, int RX, int RY, int& r,
+                                          bool& home) {
+  const int R = RX * RY;
+  unsigned* bound = counters + R;
+  while (r < R) {
+    const int rx = r % RX, ry = r / RX;
+    const int x0 = (int)((int64_t)rx * tiles_x / RX), x1 = (int)((int64_t)(rx + 1) * tiles_x / RX);
+    const int y0 = (int)((int64_t)ry * tiles_y / RY), y1 = (int)((int64_t)(ry + 1) * tiles_y / RY);
+    const int w = x1 - x0, cnt = w * (y1 - y0);
+    if (cnt > 0) {
+      const int t = (int)atomicAdd(counters + r, 1u);
+      if (t < cnt) return (y0 + t / w) * tiles_x + x0 + t % w;
+    }
+    if (home) {  // the home rectangle is done: on to the lowest one that may not be
+      home = false;
+      r = (int)*(volatile unsigned*)bound;
+      continue;
+    }
+    atomicMax(bound, (unsigned)(r + 1));
+    r = max(r + 1, (int)*(volatile unsigned*)bound);
+  }
+  return -1;
+}
+__device__ __forceinline__ int home_region(int RX, int RY) {
+  unsigned smid;
+  asm("mov.u32 %0, %%smid;" : "=r"(smid));
+  return (int)(smid % (unsigned)(RX * RY));
+}
+
 // ---------------------------------------------------------------- mrand
 // kernels/mrand.cu:3-41.
 __device__ __forceinline__ uint32_t xorshift32(uint32_t& s) {

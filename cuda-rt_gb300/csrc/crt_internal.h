@@ -122,9 +122,18 @@ __host__ __device__ inline int group_tile_w(int G) { return 32 / G >= 16 ? 8 : (
 __host__ __device__ inline int group_tile_h(int G) { return (32 / G) / group_tile_w(G); }
 constexpr int kDefaultLanesPerPixel = 4;
 
+// The persistent pixel kernels split the image's tiles into regions_x x
+// regions_y rectangles, about one per SM: a warp takes tiles from its SM's
+// rectangle (so the warps sharing an SM's L1 trace neighbouring rays), then
+// helps the others (claim_tile).  One counter per rectangle and one bound;
+// images of fewer than kMinTilesPerRegion tiles per SM keep one rectangle.
+constexpr int kMaxTileRegions = 2048;
+constexpr int kMinTilesPerRegion = 256;
+
 struct RenderArgs {
   int W, H, spp, row0, row1;
   int group;  // lanes per pixel (lanes_per_pixel)
+  int regions_x = 1, regions_y = 1;  // tile rectangles (set_tile_regions); counter holds one word per rectangle
   double angle, aspect, invW, invH, aperture, focal;
   double eye[3];
   double lpos[3], lcol[3], lradius, latt[3];
@@ -150,6 +159,11 @@ struct RenderArgs {
   double* grad_albedo = nullptr;
 };
 cudaError_t launch_render(const DScene& S, const RenderArgs& a, cudaStream_t st);
+
+// The tile rectangles for a tiles_x x tiles_y grid of tiles: with split and a
+// large enough image about num_sms() of them, near square, else one; their
+// counters and bound zeroed on st.
+cudaError_t set_tile_regions(RenderArgs& a, int tiles_x, int tiles_y, bool split, cudaStream_t st);
 
 // lens.cu: the thin-lens tables of the current device (built on first use
 // when enabled and memory allows; otherwise both NULL, and the kernels

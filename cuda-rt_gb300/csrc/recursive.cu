@@ -143,17 +143,18 @@ __global__ void __launch_bounds__(128) k_pixels_rec(DScene S, RenderArgs A, cons
   const unsigned gmask = (G == 32) ? full : (((1u << G) - 1u) << base);
   const unsigned below = gmask & ((1u << lane) - 1u);  // the lanes of my group before me
   const int tiles_x = (A.W + tw - 1) / tw, tiles_y = (A.row1 - A.row0 + th - 1) / th;
-  const int ntiles = tiles_x * tiles_y;
   const int gx = (A.W + 15) / 16;
   const D3 lpos = d3(A.lpos[0], A.lpos[1], A.lpos[2]);
   Frame fr[kMaxRecDepth];
   unsigned long long nrays = 0, nshadow = 0;  // for A.stats (accepted walks only)
   int hguess = 1;  // the hit count this lane saw in its last walk
+  int region = home_region(A.regions_x, A.regions_y);
+  bool home = true;
   while (true) {
     int tile = 0;
-    if (lane == 0) tile = (int)atomicAdd(A.counter, 1u);
+    if (lane == 0) tile = claim_tile(A.counter, tiles_x, tiles_y, A.regions_x, A.regions_y, region, home);
     tile = __shfl_sync(full, tile, 0);
-    if (tile >= ntiles) break;
+    if (tile < 0) break;
     const int pp = lane / G;  // this lane's pixel in the tile
     const int px = (tile % tiles_x) * tw + (pp % tw);
     const int py = A.row0 + (tile / tiles_x) * th + (pp / tw);
@@ -351,9 +352,12 @@ __global__ void __launch_bounds__(128) k_pixels_rec(DScene S, RenderArgs A, cons
 cudaError_t launch_render_recursive(const DScene& S, const RenderArgs& a, const DOptics* optics, int depth,
                                     cudaStream_t st) {
   if (depth < 0 || depth > kMaxRecDepth) return cudaErrorInvalidValue;
-  cudaMemsetAsync(a.counter, 0, sizeof(unsigned), st);
   RenderArgs r = a;
   r.group = depth > 0 ? lanes_per_pixel(a.spp, kRecLanesPerPixel) : 1;
+  const int tw = group_tile_w(r.group), th = group_tile_h(r.group);
+  // (one rectangle: the cost of a pixel's ray trees varies too much for rectangles of equal size)
+  cudaError_t e = set_tile_regions(r, (r.W + tw - 1) / tw, (r.row1 - r.row0 + th - 1) / th, false, st);
+  if (e != cudaSuccess) return e;
   int bps = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_pixels_rec, 128, 0);
   k_pixels_rec<<<num_sms() * (bps > 0 ? bps : 1), 128, 0, st>>>(S, r, optics, depth);

@@ -6,9 +6,13 @@
 //               traceRay (raytracer.cu:169-249), Material::shade
 //               (kernels/material.cu:6-40) and the positional Light
 //               (kernels/Light.cu:5-86); also its adjoint.  Persistent: each
-//               warp claims 8x4-pixel tiles from a counter, one pixel per
-//               lane; a lane runs its pixel's samples in order because the
-//               mrand stream couples them (a hit consumes three extra draws).
+//               warp claims tiles of 32 / G pixels (G lanes per pixel), first
+//               from its SM's rectangle of the image, then from the others;
+//               a pixel's lanes trace its samples in waves, speculating on
+//               how the mrand stream couples them (a hit consumes three
+//               extra draws).
+#include <cmath>
+
 #include "pixel.cuh"
 
 namespace crt {
@@ -63,14 +67,15 @@ __global__ void __launch_bounds__(128, 9) k_pixels(DScene S, RenderArgs A) {
   const int G = A.group, tw = group_tile_w(G), th = group_tile_h(G);
   const int tiles_x = (A.W + tw - 1) / tw;
   const int tiles_y = (A.row1 - A.row0 + th - 1) / th;
-  const int ntiles = tiles_x * tiles_y;
   const int p = lane / G;  // this lane's pixel in the tile
   unsigned pred = 0xffffffffu;
+  int region = home_region(A.regions_x, A.regions_y);
+  bool home = true;
   while (true) {
     int tile = 0;
-    if (lane == 0) tile = (int)atomicAdd(A.counter, 1u);
+    if (lane == 0) tile = claim_tile(A.counter, tiles_x, tiles_y, A.regions_x, A.regions_y, region, home);
     tile = __shfl_sync(0xffffffffu, tile, 0);
-    if (tile >= ntiles) break;
+    if (tile < 0) break;
     const int px = (tile % tiles_x) * tw + (p % tw);
     const int py = A.row0 + (tile / tiles_x) * th + (p / tw);
     pixel<MODE, kPixelsShort>(S, A, px, py, px < A.W && py < A.row1, G, pred, rb, B, D, ts, glight, ring);
@@ -88,8 +93,25 @@ static void launch_pixels(const DScene& S, const RenderArgs& a, cudaStream_t st)
   k_pixels<MODE><<<num_sms() * (bps > 0 ? bps : 1), 128, smem, st>>>(S, a);
 }
 
-cudaError_t launch_render(const DScene& S, const RenderArgs& a, cudaStream_t st) {
-  cudaMemsetAsync(a.counter, 0, sizeof(unsigned), st);
+cudaError_t set_tile_regions(RenderArgs& a, int tiles_x, int tiles_y, bool split, cudaStream_t st) {
+  int rx = 1, ry = 1;
+  const int R = min(num_sms(), kMaxTileRegions - 1);
+  if (split && (int64_t)tiles_x * tiles_y >= (int64_t)kMinTilesPerRegion * R) {
+    const double aspect = (double)max(tiles_x, 1) / (double)max(tiles_y, 1);
+    rx = (int)(std::sqrt(R * aspect) + 0.5);
+    rx = max(1, min(rx, min(R, tiles_x)));
+    ry = max(1, min((R + rx - 1) / rx, tiles_y));
+    while (rx * ry > kMaxTileRegions - 1) ry--;
+  }
+  a.regions_x = rx, a.regions_y = ry;
+  return cudaMemsetAsync(a.counter, 0, sizeof(unsigned) * (size_t)(rx * ry + 1), st);
+}
+
+cudaError_t launch_render(const DScene& S, const RenderArgs& a0, cudaStream_t st) {
+  RenderArgs a = a0;
+  const int tw = group_tile_w(a.group), th = group_tile_h(a.group);
+  cudaError_t e = set_tile_regions(a, (a.W + tw - 1) / tw, (a.row1 - a.row0 + th - 1) / th, true, st);
+  if (e != cudaSuccess) return e;
   if (a.grad_rgb)
     launch_pixels<kAdjoint>(S, a, st);
   else if (a.stats)
