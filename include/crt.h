@@ -174,7 +174,9 @@ crt_status crt_trace_shadow(crt_scene* scene, const double* rays, int64_t n, int
  * device (finite fstop) also builds that device's thin-lens tables, 2.0 GB
  * held until the process exits, when 8 GB are free and no stream capture is
  * under way (see crt_set_lens_tables; crt_set_lens_tables(0) beforehand
- * keeps them off). */
+ * keeps them off).  The renders of one scene (crt_render,
+ * crt_render_recursive, crt_adjoint_lambert) share the scene's tile
+ * counters: issue them on one stream, or order them, never overlapping. */
 crt_status crt_render(crt_scene* scene, const crt_camera* camera, const crt_light* light,
                       const crt_render_params* params, const crt_render_out* out, void* stream);
 
