@@ -315,6 +315,37 @@ def run_build_only(args):
             "build_mtris_s": round(n / ms / 1e3, 1), "gpu_launches": build_launches(n) * args.steps}
 
 
+def run_render_only(args, width, height):
+    """crt_render of the large mesh (thin lens, 16 spp) at width x height with
+    a device output, W untimed then K timed back to back: a smaller frame of
+    the same kernel, for multi-pass profiling (about 2.4 GB on the device
+    with the lens tables)."""
+    import torch
+
+    import crt
+    from crt import data
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    sc = data.config1()
+    scene = crt.Scene(sc.mesh)
+    stream = torch.cuda.current_stream()
+    rgb = torch.empty((width * height, 3), dtype=torch.uint8, device="cuda")
+    for _ in range(max(args.warmup, 1)):
+        scene.render(sc.camera, sc.light, width, height, SPP, out={"rgb8": rgb}, stream=stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        scene.render(sc.camera, sc.light, width, height, SPP, out={"rgb8": rgb}, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    scene.check()
+    ms = e0.elapsed_time(e1) / max(args.steps, 1)
+    rays = width * height * SPP
+    return {"metric": "render ms (large mesh, back to back)", "value": round(ms, 4), "unit": "ms",
+            "higher_is_better": False, "steps": args.steps, "warmup": args.warmup, "width": width, "height": height,
+            "spp": SPP, "mrays_s": round(rays / ms / 1e3, 1), "gpu_launches": args.steps}
+
+
 def run_batched_only(count):
     """The first `count` meshes of the batched workload, built and rendered
     twice in the two-launch form with a fixed shape; the second run timed."""
@@ -720,6 +751,8 @@ def main():
     ap.add_argument("--batched-only", type=int, default=0, metavar="MESHES",
                     help="build and render the first MESHES meshes of the batched workload twice, two launches "
                          "each (block 256, 1 lane per pixel, stack 16), and time the second run: for profiling")
+    ap.add_argument("--render-only", type=int, nargs=2, default=None, metavar=("WIDTH", "HEIGHT"),
+                    help="time crt_render of the large mesh alone at WIDTH x HEIGHT, 16 spp: for profiling it")
     ap.add_argument("--build-only", action="store_true",
                     help="time the LBVH build of the large mesh alone (no render, no lens tables): for profiling it")
     args = ap.parse_args()
@@ -734,6 +767,8 @@ def main():
         barrier(dist)
         if args.build_only:
             line = run_build_only(args)
+        elif args.render_only:
+            line = run_render_only(args, *args.render_only)
         elif args.batched_only:
             line = run_batched_only(args.batched_only)
         else:
